@@ -1,0 +1,387 @@
+"""Benchmark: windows/s of the batched HDBSCAN forward on one GB300.
+
+Default workload (the config the headline metric is quoted on): 256 windows x
+1024 points x 16 dims float32, mcs=ms=2, eps=0.1 (seeded Gaussian mixtures
+standing in for the reference's private corpus; hdbscan_gb300/synthetic.py).
+
+A step = one pass of the whole pipeline over the batch:
+  value  device-resident: replay of the CUDA graph that holds the persistent
+         ragged launch (inputs already in HBM), CUDA events per step, L2
+         flushed (256 MiB write) between steps outside the events.
+  e2e    the public hdbscan() call on a pinned host array: H2D of X, the
+         forward, the status read and D2H of the labels inside the timing.
+Also reported: the plain per-window launch of the same kernels (one launch per
+window, no graph), labels bit-exact against the graph run and the oracle,
+the forward kernel's roofline, and the CPU oracle on the host cores.
+
+`--impl reference` times the reference's own kernel code compiled for the CPU
+(oracle/_ref) or, if that is absent, the oracle restatement, on all host
+threads, same workload/metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIG_NAMES = {"c2": "uniform batch [256,1024,16] float32 mcs=ms=2 eps=0.1",
+                "c1": "single window [1,512,8] float64 mcs=ms=5",
+                "c3": "ragged 512 windows N~logU[64,4096] D=32 mcs=ms=10 eps=0.05",
+                "c4": "[64,2048,64] float32 mcs=15 ms=5",
+                "c5": "ragged 96 windows N~U[2048,4096] D=128 float64 mcs=32 ms=16"}
+
+
+def load_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.file = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.file.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_batch(packed, offsets, params, threads, prefer_reference=True):
+    """Run the CPU implementation on the given windows; returns (labels, kind)."""
+    import ctypes
+
+    from oracle import oracle
+
+    precision = params["precision"]
+    mcs, ms, eps = params["min_cluster_size"], params["min_samples"], params["cluster_selection_epsilon"]
+    ref_lib = ROOT / "oracle" / "_ref" / "libhdb_ref.so"
+    if prefer_reference:
+        try:
+            from oracle import build_ref
+
+            build_ref.build()
+        except Exception:
+            pass
+    if prefer_reference and ref_lib.exists():
+        lib = ctypes.CDLL(str(ref_lib))
+        suffix = "f32" if precision == "float32" else "f64"
+        fn = getattr(lib, f"hdb_ref_batch_{suffix}")
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                       ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        dtype = np.float32 if precision == "float32" else np.float64
+        x = np.ascontiguousarray(packed, dtype=dtype)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        labels = np.empty(int(off[-1]), np.int32)
+        status = np.zeros(len(off) - 1, np.int32)
+        fn(x.ctypes.data, off.ctypes.data, len(off) - 1, x.shape[1], mcs, ms, eps, labels.ctypes.data,
+           status.ctypes.data, threads)
+        return labels, "reference"
+    labels, _ = oracle.batch(packed, offsets, mcs, ms, eps, precision, threads=threads)
+    return labels, "port"
+
+
+def sample_windows(offsets, target_windows):
+    count = min(len(offsets) - 1, target_windows)
+    return offsets[: count + 1].copy(), count
+
+
+def run_reference_arm(args, packed, offsets, params):
+    threads = len(os.sched_getaffinity(0))
+    sub_offsets, count = sample_windows(offsets, args.cpu_windows)
+    sub = packed[: int(sub_offsets[-1])]
+    times = []
+    kind = "port"
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, kind = cpu_reference_batch(sub, sub_offsets, params, threads)
+        elapsed = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(elapsed)
+    per_step = statistics.median(times)
+    value = count / per_step
+    line = {
+        "impl": "reference", "metric": "windows_per_s", "value": value, "unit": "windows/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if params["precision"] == "float32" else "f64",
+        "data": "synthetic", "config": {"workload": CONFIG_NAMES[args.config], "windows_timed": count},
+        "cpu_baseline": {"value": value, "unit": "windows/s", "cores": threads, "kind": kind,
+                         "sample": f"first {count} windows of the workload per step"},
+        "e2e": {"value": value, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    parser = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=20)
+    parser.add_argument("--warmup", type=int, default=5)
+    parser.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    parser.add_argument("--config", choices=sorted(CONFIG_NAMES), default="c2")
+    parser.add_argument("--cpu-windows", type=int, default=256)
+    parser.add_argument("--plain-passes", type=int, default=2)
+    parser.add_argument("--skip-cpu", action="store_true")
+    args = parser.parse_args()
+    if args.warmup < 3:
+        parser.error("--warmup must be >= 3")
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from hdbscan_gb300 import synthetic
+
+    packed64, offsets, params = synthetic.make(args.config)
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference_arm(args, packed64, offsets, params)
+        return
+
+    import torch
+
+    import hdbscan_gb300
+    from hdbscan_gb300 import _lib
+    from hdbscan_gb300._cuda import Plan, raise_for_status
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    precision = params["precision"]
+    dtype = torch.float32 if precision == "float32" else torch.float64
+    np_dtype = np.float32 if precision == "float32" else np.float64
+    mcs, ms, eps = params["min_cluster_size"], params["min_samples"], params["cluster_selection_epsilon"]
+    B = len(offsets) - 1
+    T = int(offsets[-1])
+    D = packed64.shape[1]
+    host = np.ascontiguousarray(packed64, dtype=np_dtype)
+    X = torch.from_numpy(host).to(device)
+
+    plan = Plan(offsets, D, min_cluster_size=mcs, min_samples=ms, cluster_selection_epsilon=eps,
+                precision=precision)
+    workspace = plan.workspace()
+    labels, status = plan.capture(X, workspace=workspace)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    # Warm-up + correctness of the graph run.
+    for _ in range(args.warmup):
+        plan.replay()
+    torch.cuda.synchronize()
+    raise_for_status(int(status.item()))
+    graph_labels = labels.cpu().numpy().copy()
+
+    # ---- timed: graph replay, device resident ------------------------------
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            plan.replay()
+            end.record(stream)
+            end.synchronize()
+            step_ms.append(start.elapsed_time(end))
+    torch.cuda.synchronize()
+    ms_per_step = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms_per_step], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    value = B * world / (ms_per_step / 1e3)
+
+    # ---- kernel-only timing of the forward kernel (non-graph launch) --------
+    kernel_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.fill_(1)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        plan.forward(X, labels=labels, workspace=workspace, status=status)
+        end.record(stream)
+        end.synchronize()
+        kernel_ms.append(start.elapsed_time(end))
+    kernel_ms_mean = float(np.mean(kernel_ms))
+
+    # ---- plain per-window launches of the same kernels ----------------------
+    plain_plans = {}
+    plain_labels = torch.empty(T, dtype=torch.int32, device=device)
+    one_ws = {}
+    for w in range(B):
+        n = int(offsets[w + 1] - offsets[w])
+        if n not in plain_plans:
+            plain_plans[n] = Plan(np.array([0, n]), D, min_cluster_size=mcs, min_samples=ms,
+                                  cluster_selection_epsilon=eps, precision=precision)
+            one_ws[n] = plain_plans[n].workspace()
+    plain_status = torch.empty(1, dtype=torch.int32, device=device)
+
+    def plain_pass():
+        for w in range(B):
+            lo, hi = int(offsets[w]), int(offsets[w + 1])
+            p = plain_plans[hi - lo]
+            p.forward(X[lo:hi], labels=plain_labels[lo:hi], workspace=one_ws[hi - lo], status=plain_status)
+
+    plain_pass()
+    torch.cuda.synchronize()
+    plain_ms = []
+    for _ in range(args.plain_passes):
+        flush.fill_(1)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        plain_pass()
+        end.record(stream)
+        end.synchronize()
+        plain_ms.append(start.elapsed_time(end))
+    plain_value = B / (float(np.mean(plain_ms)) / 1e3)
+    plain_exact = bool(np.array_equal(plain_labels.cpu().numpy(), graph_labels))
+
+    # ---- end to end through the public API ----------------------------------
+    pinned = torch.from_numpy(host).pin_memory()
+    uniform = len(set(np.diff(offsets).tolist())) == 1
+    e2e_ms = []
+    for step in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if uniform:
+            n = int(offsets[1])
+            result = hdbscan_gb300.hdbscan(pinned.view(B, n, D).to(device, non_blocking=True),
+                                           min_cluster_size=mcs, min_samples=ms,
+                                           cluster_selection_epsilon=eps, backend="cuda", precision=precision)
+        else:
+            result, _ = hdbscan_gb300.hdbscan_ragged(packed=pinned.to(device, non_blocking=True), offsets=offsets,
+                                                     min_cluster_size=mcs, min_samples=ms,
+                                                     cluster_selection_epsilon=eps, precision=precision)
+        out = result.cpu()
+        if step >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_exact = bool(np.array_equal(out.numpy().reshape(-1), graph_labels))
+    e2e_value = B / (float(np.median(e2e_ms)) / 1e3)
+
+    # ---- oracle parity on a sample + CPU baseline ---------------------------
+    from oracle import oracle
+
+    sample = list(range(0, B, max(1, B // 8)))[:8]
+    oracle_exact = True
+    for w in sample:
+        lo, hi = int(offsets[w]), int(offsets[w + 1])
+        o = oracle.cluster(host[lo:hi], mcs, ms, eps, precision)
+        oracle_exact &= bool(np.array_equal(o["labels"], graph_labels[lo:hi]))
+    cpu = None
+    if not args.skip_cpu and rank == 0:
+        threads = len(os.sched_getaffinity(0))
+        sub_offsets, count = sample_windows(offsets, args.cpu_windows)
+        t0 = time.perf_counter()
+        _, kind = cpu_reference_batch(host[: int(sub_offsets[-1])], sub_offsets, params, threads,
+                                      prefer_reference=False)
+        elapsed = time.perf_counter() - t0
+        cpu = {"value": count / elapsed, "unit": "windows/s", "cores": threads, "kind": kind,
+               "sample": f"first {count} of {B} windows, oracle restatement on {threads} host threads"}
+
+    # ---- roofline of the forward kernel -------------------------------------
+    peak, peak_kind = load_peaks()
+    itemsize = 4 if precision == "float32" else 8
+    sizes = np.diff(offsets)
+    describe = json.loads(plan.describe())
+    matrix = any(c["variant"] == "matrix" for c in describe["classes"])
+    # Algorithmic bytes per launch: read X (N*D*s) + write labels (4N) per window,
+    # plus the N^2*s distance block read when the matrix variant is used.
+    algo_bytes = float(np.sum(sizes * D * itemsize + sizes * 4))
+    if matrix:
+        algo_bytes += float(np.sum(sizes.astype(np.float64) ** 2 * itemsize))
+    achieved = algo_bytes / (kernel_ms_mean / 1e3) / 1e9
+    traffic = None
+    traffic_path = ROOT / "profiles" / f"traffic_{args.config}.json"
+    if traffic_path.exists():
+        traffic = json.loads(traffic_path.read_text()).get("dram_bytes_per_launch")
+    launches_per_step = len(describe["classes"]) + len(describe["core"]) + (1 if describe["distance_tiles"] else 0)
+    line = {
+        "metric": "windows_per_s", "value": value, "unit": "windows/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if precision == "float32" else "f64", "data": "synthetic",
+        "config": {"workload": CONFIG_NAMES[args.config], "windows": B, "points": T, "dims": D,
+                   "l2": "256 MiB flush between timed steps", "graph": True, "parallelism": "replicas"},
+        "points_per_s": T * world / (ms_per_step / 1e3),
+        "plain_per_window": {"value": plain_value, "unit": "windows/s", "labels_bit_exact": plain_exact},
+        "speedup_vs_plain": value / plain_value,
+        "labels_bit_exact": {"graph_vs_oracle_sample": oracle_exact, "e2e_vs_graph": e2e_exact},
+        "e2e": {"value": e2e_value, "unit": "windows/s", "h2d_bytes_per_step": int(host.nbytes),
+                "d2h_bytes_per_step": int(T * 4 + 4)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "hdb_forward_kernel", "kernel_ms": kernel_ms_mean,
+                     "note": "latency-bound (serial Prim/tree chains); algorithmic bytes per launch"},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "plan": describe["classes"],
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,48 @@
+"""Ragged batches: windows of different sizes in one persistent launch."""
+
+from __future__ import annotations
+
+import numpy as np
+
+from ._api import validate_limits, validate_parameters
+
+
+def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=5, min_samples=None,
+                   cluster_selection_epsilon=0.0, precision="float32", return_hierarchy=False,
+                   force_matrix=False):
+    """Cluster a ragged batch in one launch.
+
+    Give either `windows` (a list of [N_i, D] arrays/tensors) or `packed`
+    ([sum N_i, D]) with `offsets` ([B+1] row offsets).  Returns
+    (labels [sum N_i] int32 CUDA tensor, offsets) and, with
+    return_hierarchy=True, a dict of device exports (Prim edges, sort order,
+    single-linkage rows, condensed clusters, cores).
+    """
+    min_cluster_size, min_samples, cluster_selection_epsilon = validate_parameters(
+        min_cluster_size, min_samples, cluster_selection_epsilon, "cuda", precision)
+    from ._cuda import cluster_ragged, pack, to_device_tensor
+
+    if windows is not None:
+        if packed is not None or offsets is not None:
+            raise ValueError("give either windows or packed+offsets")
+        packed, offsets = pack(windows, precision)
+    else:
+        if packed is None or offsets is None:
+            raise ValueError("give either windows or packed+offsets")
+        packed = to_device_tensor(packed, precision)
+        offsets = np.asarray(offsets, dtype=np.int64)
+    if packed.ndim != 2 or packed.shape[1] < 1:
+        raise ValueError("X requires nonempty batches/features and at least 2 samples")
+    sizes = np.diff(offsets)
+    if len(sizes) < 1 or offsets[0] != 0 or offsets[-1] != packed.shape[0] or sizes.min() < 2:
+        raise ValueError("X requires nonempty batches/features and at least 2 samples")
+    validate_limits(int(sizes.max()), min_cluster_size, min_samples, cluster_selection_epsilon, precision)
+    if min_samples > int(sizes.min()):
+        raise ValueError("min_samples must not exceed the number of samples")
+    result = cluster_ragged(packed, offsets, int(min_cluster_size), int(min_samples),
+                            float(cluster_selection_epsilon), precision, exports=return_hierarchy,
+                            force_matrix=force_matrix)
+    if return_hierarchy:
+        labels, exports = result
+        return labels, offsets, exports
+    return result, offsets

@@ -1,0 +1,674 @@
+// C ABI and host plan layer (include/hdbscan_gb300.h).
+//
+// A plan turns a ragged batch description into: per-window kernel variants
+// (the autotune table in choose_variant), window classes launched as
+// persistent grids over size-sorted queues on forked streams, the tile and
+// row work lists of the distance/core kernels, and one pinned host image of
+// every device table, uploaded by a single cudaMemcpyAsync per call so the
+// whole forward is capturable in a CUDA graph.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hdbscan_gb300.h"
+#include "hdb_args.h"
+#include "hdb_registry.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& message) {
+    g_error = message;
+    return code;
+}
+
+#define HDB_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(HDB_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct WindowClass {
+    const hdb::ForwardVariant* fv = nullptr;
+    int x_in_smem = 0;
+    std::vector<int> windows;  // descending n
+    int nmax = 0;
+    size_t smem = 0;
+    int grid = 0;
+    size_t queue_off = 0;      // element offset into the queue table
+    int ticket = 0;            // index into the ticket table
+};
+
+struct CoreLaunch {
+    const hdb::CoreVariant* cv = nullptr;  // null = select kernel
+    bool matrix = false;
+    std::vector<int32_t> items;             // (window, row) pairs
+    size_t items_off = 0;                   // byte offset in tables
+    size_t select_smem = 0;
+};
+
+}  // namespace
+
+struct hdb_plan {
+    int precision = 0;
+    int B = 0;
+    int D = 0;
+    int mcs = 2;
+    int ms = 1;
+    double eps = 0;
+    unsigned flags = 0;
+    int device = 0;
+    int sms = 0;
+    int64_t T = 0;
+    std::vector<int64_t> offsets;
+    const hdb::PrecisionKernels* k = nullptr;
+    std::vector<WindowClass> classes;
+    std::vector<CoreLaunch> cores;
+    std::vector<int32_t> tiles;             // (window, ti, tj)
+    std::vector<int64_t> dist_offsets;      // per window (elements), -1 if not materialized
+    int64_t dist_elems = 0;
+    // Table layout (byte offsets within the workspace).
+    size_t t_offsets = 0, t_dist_off = 0, t_queue = 0, t_tickets = 0, t_tiles = 0, t_edge_window = 0;
+    size_t tables_bytes = 0;
+    size_t w_core = 0, w_core_nbr = 0, w_dist = 0, ws_bytes = 0;
+    unsigned char* h_tables = nullptr;      // pinned
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> events;
+    cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
+
+// Autotune table: (threads, vertices per thread) by window size, register
+// dimensions by D.  Windows whose coordinates do not fit the register budget
+// of an instantiated variant use the matrix variant.
+const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int precision, int n, int D,
+                                          bool force_matrix) {
+    int threads, v;
+    if (n <= 128) { threads = 128; v = 1; }
+    else if (n <= 256) { threads = 256; v = 1; }
+    else if (n <= 512) { threads = 512; v = 1; }
+    else if (n <= 1024) { threads = 512; v = 2; }
+    else if (n <= 2048) { threads = 1024; v = 2; }
+    else { threads = 1024; v = 4; }
+    int dp = 0;
+    if (!force_matrix) {
+        const int options32[] = {8, 16, 32};
+        const int options64[] = {8, 16};
+        const int* options = precision == HDB_F32 ? options32 : options64;
+        const int count = precision == HDB_F32 ? 3 : 2;
+        for (int i = 0; i < count; ++i)
+            if (D <= options[i]) { dp = options[i]; break; }
+    }
+    const hdb::ForwardVariant* fallback = nullptr;
+    for (int i = 0; i < k.n_forward; ++i) {
+        const hdb::ForwardVariant& f = k.forward[i];
+        if (f.threads != threads || f.v != v) continue;
+        if (f.dp == dp) return &f;
+        if (f.dp == 0) fallback = &f;
+    }
+    return fallback;
+}
+
+const hdb::CoreVariant* choose_core(const hdb::PrecisionKernels& k, int precision, int ms, int D, bool matrix) {
+    int K = 0;
+    for (int c : {8, 16, 32, 64})
+        if (ms <= c) { K = c; break; }
+    if (!K) return nullptr;
+    int dp = 0;
+    if (!matrix) {
+        const int limit = precision == HDB_F32 ? 64 : 32;
+        for (int c : {8, 16, 32, 64})
+            if (D <= c && c <= limit) { dp = c; break; }
+        if (!dp) return nullptr;
+    }
+    for (int i = 0; i < k.n_core; ++i)
+        if (k.core[i].k == K && k.core[i].dp == dp) return &k.core[i];
+    return nullptr;
+}
+
+template <typename T>
+size_t put(std::vector<unsigned char>& image, size_t& cursor, const std::vector<T>& values) {
+    cursor = align_up(cursor, 256);
+    const size_t at = cursor;
+    const size_t bytes = values.size() * sizeof(T);
+    if (image.size() < at + bytes) image.resize(at + bytes);
+    if (bytes) std::memcpy(image.data() + at, values.data(), bytes);
+    cursor = at + bytes;
+    return at;
+}
+
+int build_plan(hdb_plan* p) {
+    const hdb::PrecisionKernels& k = *p->k;
+    const bool unit = p->ms <= 2;
+    const bool force_matrix = (p->flags & HDB_FLAG_FORCE_MATRIX) != 0;
+    int optin = 0;
+    HDB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+    HDB_CUDA(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
+
+    // ---- classes ------------------------------------------------------------
+    std::vector<int> order(p->B);
+    for (int w = 0; w < p->B; ++w) order[w] = w;
+    auto size_of = [&](int w) { return (int)(p->offsets[w + 1] - p->offsets[w]); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return size_of(a) > size_of(b); });
+    for (int w : order) {
+        const int n = size_of(w);
+        const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, force_matrix);
+        if (!fv) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(n) + " points");
+        const bool static_ok = true;
+        (void)static_ok;
+        int xs = fv->dp > 0 ? 1 : 0;
+        size_t smem = k.forward_smem(n, fv->dp, xs, unit);
+        const size_t budget = (size_t)optin - 2048;  // leave room for static shared memory
+        if (smem > budget && xs) { xs = 0; smem = k.forward_smem(n, fv->dp, false, unit); }
+        if (smem > budget)
+            return fail(HDB_E_INVALID, "window of " + std::to_string(n) + " points exceeds shared memory");
+        WindowClass* cls = nullptr;
+        for (auto& c : p->classes)
+            if (c.fv == fv && c.x_in_smem == xs) { cls = &c; break; }
+        if (!cls) {
+            p->classes.emplace_back();
+            cls = &p->classes.back();
+            cls->fv = fv;
+            cls->x_in_smem = xs;
+        }
+        cls->windows.push_back(w);
+        cls->nmax = std::max(cls->nmax, n);
+    }
+    std::stable_sort(p->classes.begin(), p->classes.end(),
+                     [](const WindowClass& a, const WindowClass& b) { return a.nmax > b.nmax; });
+
+    // ---- distance blocks and tiles for matrix-variant windows --------------
+    p->dist_offsets.assign(p->B, -1);
+    p->dist_elems = 0;
+    for (auto& c : p->classes) {
+        if (c.fv->dp != 0) continue;
+        for (int w : c.windows) {
+            const int n = size_of(w);
+            const int64_t ld = (n + 3) & ~3;
+            p->dist_offsets[w] = p->dist_elems;
+            p->dist_elems += align_up((size_t)(n * ld), 64);
+            const int t = (n + 63) / 64;
+            for (int ti = 0; ti < t; ++ti)
+                for (int tj = ti; tj < t; ++tj) {
+                    p->tiles.push_back(w);
+                    p->tiles.push_back(ti);
+                    p->tiles.push_back(tj);
+                }
+        }
+    }
+
+    // ---- core distances -----------------------------------------------------
+    if (!unit) {
+        for (int pass = 0; pass < 2; ++pass) {
+            const bool matrix = pass == 1;
+            CoreLaunch launch;
+            launch.matrix = matrix;
+            launch.cv = choose_core(k, p->precision, p->ms, p->D, matrix);
+            CoreLaunch select;
+            select.matrix = matrix;
+            int nmax = 0;
+            for (auto& c : p->classes) {
+                if ((c.fv->dp == 0) != matrix) continue;
+                for (int w : c.windows) {
+                    const int n = size_of(w);
+                    nmax = std::max(nmax, n);
+                    if (launch.cv) {
+                        for (int r = 0; r < n; r += 128) { launch.items.push_back(w); launch.items.push_back(r); }
+                    } else {
+                        for (int r = 0; r < n; ++r) { select.items.push_back(w); select.items.push_back(r); }
+                    }
+                }
+            }
+            if (!launch.items.empty()) p->cores.push_back(launch);
+            if (!select.items.empty()) {
+                select.select_smem = (size_t)nmax * (size_t)real_bytes(p->precision);
+                p->cores.push_back(select);
+            }
+        }
+    }
+
+    // ---- grids --------------------------------------------------------------
+    for (auto& c : p->classes) {
+        c.smem = k.forward_smem(c.nmax, c.fv->dp, c.x_in_smem, unit);
+        HDB_CUDA(cudaFuncSetAttribute(c.fv->func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
+        int per_sm = 0;
+        HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads, c.smem));
+        if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
+        c.grid = (int)std::min<size_t>(c.windows.size(), (size_t)per_sm * p->sms);
+    }
+    for (auto& c : p->cores)
+        if (!c.cv && c.select_smem > 48 * 1024)
+            HDB_CUDA(cudaFuncSetAttribute(k.select_func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)c.select_smem));
+
+    // ---- table image --------------------------------------------------------
+    std::vector<unsigned char> image;
+    size_t cursor = 0;
+    p->t_offsets = put(image, cursor, p->offsets);
+    p->t_dist_off = put(image, cursor, p->dist_offsets);
+    std::vector<int32_t> queue;
+    std::vector<int32_t> tickets(p->classes.size(), 0);
+    for (size_t i = 0; i < p->classes.size(); ++i) {
+        auto& c = p->classes[i];
+        c.queue_off = queue.size();
+        c.ticket = (int)i;
+        queue.insert(queue.end(), c.windows.begin(), c.windows.end());
+    }
+    p->t_queue = put(image, cursor, queue);
+    p->t_tickets = put(image, cursor, tickets);
+    p->t_tiles = put(image, cursor, p->tiles);
+    for (auto& c : p->cores) c.items_off = put(image, cursor, c.items);
+    std::vector<int32_t> edge_window;
+    edge_window.reserve((size_t)(p->T - p->B));
+    for (int w = 0; w < p->B; ++w)
+        for (int i = 0; i < size_of(w) - 1; ++i) edge_window.push_back(w);
+    p->t_edge_window = put(image, cursor, edge_window);
+    p->tables_bytes = align_up(std::max<size_t>(cursor, 256), 256);
+    image.resize(p->tables_bytes, 0);
+    HDB_CUDA(cudaMallocHost((void**)&p->h_tables, p->tables_bytes));
+    std::memcpy(p->h_tables, image.data(), p->tables_bytes);
+
+    // ---- workspace layout ---------------------------------------------------
+    size_t ws = p->tables_bytes;
+    const size_t rb = (size_t)real_bytes(p->precision);
+    p->w_core = ws = align_up(ws, 256);
+    if (!unit) ws += (size_t)p->T * rb;
+    p->w_core_nbr = ws = align_up(ws, 256);
+    if (!unit) ws += (size_t)p->T * sizeof(int32_t);
+    p->w_dist = ws = align_up(ws, 256);
+    ws += (size_t)p->dist_elems * rb;
+    p->ws_bytes = align_up(std::max<size_t>(ws, 256), 256);
+
+    // ---- streams for concurrent classes ------------------------------------
+    const bool fork = !(p->flags & HDB_FLAG_NO_GRAPH_STREAMS) && p->classes.size() > 1;
+    if (fork) {
+        for (size_t i = 1; i < p->classes.size(); ++i) {
+            cudaStream_t s;
+            HDB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            p->aux.push_back(s);
+        }
+        for (size_t i = 0; i < p->classes.size(); ++i) {
+            cudaEvent_t e;
+            HDB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            p->events.push_back(e);
+        }
+    }
+    return HDB_OK;
+}
+
+int check_device(const hdb_plan* p) {
+    int device = -1;
+    HDB_CUDA(cudaGetDevice(&device));
+    if (device != p->device)
+        return fail(HDB_E_DEVICE, "plan was created on device " + std::to_string(p->device) + " but device " +
+                                      std::to_string(device) + " is current");
+    return HDB_OK;
+}
+
+int check_workspace(const hdb_plan* p, void* ws, size_t bytes) {
+    if (!ws) return fail(HDB_E_WORKSPACE, "workspace is NULL");
+    if (bytes < p->ws_bytes)
+        return fail(HDB_E_WORKSPACE, "workspace of " + std::to_string(bytes) + " bytes is smaller than the " +
+                                         std::to_string(p->ws_bytes) + " bytes the plan needs");
+    if (reinterpret_cast<uintptr_t>(ws) % 256)
+        return fail(HDB_E_WORKSPACE, "workspace must be 256-byte aligned");
+    return HDB_OK;
+}
+
+int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t* status,
+                const hdb_exports_t* ex, cudaStream_t stream) {
+    const hdb::PrecisionKernels& k = *p->k;
+    unsigned char* ws = static_cast<unsigned char*>(ws_v);
+    const bool unit = p->ms <= 2;
+    hdb_exports_t none;
+    std::memset(&none, 0, sizeof(none));
+    if (!ex) ex = &none;
+    HDB_CUDA(cudaMemcpyAsync(ws, p->h_tables, p->tables_bytes, cudaMemcpyHostToDevice, stream));
+    if (status) HDB_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), stream));
+    const int64_t* d_offsets = reinterpret_cast<const int64_t*>(ws + p->t_offsets);
+    const int64_t* d_dist_off = reinterpret_cast<const int64_t*>(ws + p->t_dist_off);
+    void* dist = ws + p->w_dist;
+    void* core = ex->core ? ex->core : (void*)(ws + p->w_core);
+    int32_t* core_nbr = ex->core_nbr ? ex->core_nbr : reinterpret_cast<int32_t*>(ws + p->w_core_nbr);
+
+    if (!p->tiles.empty()) {
+        hdb::DistanceArgs a{};
+        a.X = X;
+        a.offsets = d_offsets;
+        a.tiles = reinterpret_cast<const int32_t*>(ws + p->t_tiles);
+        a.n_tiles = (int)(p->tiles.size() / 3);
+        a.D = p->D;
+        a.dist = dist;
+        a.dist_offsets = d_dist_off;
+        a.status = status;
+        k.launch_distance(a, a.n_tiles, stream);
+        HDB_CUDA(cudaGetLastError());
+    }
+    for (const auto& c : p->cores) {
+        hdb::CoreArgs a{};
+        a.X = X;
+        a.offsets = d_offsets;
+        a.items = reinterpret_cast<const int32_t*>(ws + c.items_off);
+        a.n_items = (int)(c.items.size() / 2);
+        a.D = p->D;
+        a.ms = p->ms;
+        a.dist = c.matrix ? dist : nullptr;
+        a.dist_offsets = d_dist_off;
+        a.core = core;
+        a.core_nbr = core_nbr;
+        a.status = status;
+        if (c.cv) c.cv->launch(a, a.n_items, stream);
+        else k.launch_select(a, a.n_items, c.select_smem, stream);
+        HDB_CUDA(cudaGetLastError());
+    }
+    const bool fork = !p->aux.empty();
+    if (fork) {
+        HDB_CUDA(cudaEventRecord(p->events[0], stream));
+        for (auto s : p->aux) HDB_CUDA(cudaStreamWaitEvent(s, p->events[0], 0));
+    }
+    for (size_t i = 0; i < p->classes.size(); ++i) {
+        const WindowClass& c = p->classes[i];
+        hdb::ForwardArgs a{};
+        a.X = X;
+        a.offsets = d_offsets;
+        a.queue = reinterpret_cast<const int32_t*>(ws + p->t_queue) + c.queue_off;
+        a.queue_len = (int)c.windows.size();
+        a.ticket = reinterpret_cast<int32_t*>(ws + p->t_tickets) + c.ticket;
+        a.D = p->D;
+        a.mcs = p->mcs;
+        a.unit_core = unit ? 1 : 0;
+        a.x_in_smem = c.x_in_smem;
+        a.eps = p->eps;
+        a.core = unit ? nullptr : core;
+        a.dist = dist;
+        a.dist_offsets = d_dist_off;
+        a.labels = labels;
+        a.status = status;
+        a.edges_uv = ex->edges_uv;
+        a.edge_w = ex->edge_w;
+        a.order = ex->order;
+        a.link_lr = ex->link_lr;
+        a.link_w = ex->link_w;
+        a.link_size = ex->link_size;
+        if (a.link_lr && (!a.link_w || !a.link_size)) return fail(HDB_E_INVALID, "link_lr needs link_w and link_size");
+        if (a.edges_uv && !a.edge_w) return fail(HDB_E_INVALID, "edges_uv needs edge_w");
+        a.n_clusters = ex->n_clusters;
+        a.cl_parent = ex->cl_parent;
+        a.cl_birth = ex->cl_birth;
+        a.cl_stability = ex->cl_stability;
+        a.cl_selected = ex->cl_selected;
+        a.point_parent = ex->point_parent;
+        if (a.cl_parent && (!a.cl_birth || !a.cl_stability || !a.cl_selected || !a.point_parent || !a.n_clusters))
+            return fail(HDB_E_INVALID, "cl_parent needs cl_birth, cl_stability, cl_selected, point_parent, n_clusters");
+        cudaStream_t s = (fork && i > 0) ? p->aux[i - 1] : stream;
+        c.fv->launch(a, c.grid, c.smem, s);
+        HDB_CUDA(cudaGetLastError());
+    }
+    if (fork) {
+        for (size_t i = 1; i < p->classes.size(); ++i) {
+            HDB_CUDA(cudaEventRecord(p->events[i], p->aux[i - 1]));
+            HDB_CUDA(cudaStreamWaitEvent(stream, p->events[i], 0));
+        }
+    }
+    return HDB_OK;
+}
+
+// ---- plan cache of the dense seam -----------------------------------------
+struct CacheKey {
+    int precision, batch, n, dims, mcs, ms, device;
+    uint64_t eps_bits;
+    bool operator==(const CacheKey& o) const {
+        return precision == o.precision && batch == o.batch && n == o.n && dims == o.dims && mcs == o.mcs &&
+               ms == o.ms && device == o.device && eps_bits == o.eps_bits;
+    }
+};
+std::mutex g_cache_mutex;
+std::list<std::pair<CacheKey, hdb_plan*>> g_cache;
+
+int cached_plan(int precision, int batch, int n, int dims, int mcs, int ms, double eps, hdb_plan** out) {
+    int device = 0;
+    HDB_CUDA(cudaGetDevice(&device));
+    CacheKey key{precision, batch, n, dims, mcs, ms, device, 0};
+    std::memcpy(&key.eps_bits, &eps, sizeof(eps));
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    for (auto it = g_cache.begin(); it != g_cache.end(); ++it) {
+        if (it->first == key) {
+            g_cache.splice(g_cache.begin(), g_cache, it);
+            *out = it->second;
+            return HDB_OK;
+        }
+    }
+    if ((int64_t)batch * n > INT32_MAX) return fail(HDB_E_INVALID, "batch * n exceeds int32");
+    std::vector<int64_t> offsets((size_t)batch + 1);
+    for (int b = 0; b <= batch; ++b) offsets[b] = (int64_t)b * n;
+    hdb_plan* p = nullptr;
+    int rc = hdb_plan_create(&p, precision, batch, offsets.data(), dims, mcs, ms, eps, 0);
+    if (rc) return rc;
+    g_cache.emplace_front(key, p);
+    if (g_cache.size() > 16) {
+        hdb_plan_destroy(g_cache.back().second);
+        g_cache.pop_back();
+    }
+    *out = p;
+    return HDB_OK;
+}
+
+int cluster_dense(int precision, const void* X, int batch, int n, int dims, int mcs, int ms, double eps,
+                  int32_t* labels, void* ws, size_t ws_bytes, int32_t* status, void* stream) {
+    hdb_plan* p = nullptr;
+    int rc = cached_plan(precision, batch, n, dims, mcs, ms, eps, &p);
+    if (rc) return rc;
+    return hdb_plan_forward(p, X, labels, ws, ws_bytes, status, nullptr, stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int hdb_version(void) { return HDB_VERSION; }
+
+const char* hdb_last_error(void) { return g_error.c_str(); }
+
+int hdb_plan_create(hdb_plan_t** out, int precision, int windows, const int64_t* offsets_host, int dims,
+                    int min_cluster_size, int min_samples, double epsilon, unsigned flags) {
+    if (!out) return fail(HDB_E_INVALID, "plan output pointer is NULL");
+    *out = nullptr;
+    if (precision != HDB_F32 && precision != HDB_F64)
+        return fail(HDB_E_INVALID, "precision must be 'float32' or 'float64'");
+    if (windows < 1 || dims < 1 || !offsets_host)
+        return fail(HDB_E_INVALID, "X requires nonempty batches/features and at least 2 samples");
+    if (min_cluster_size < 2) return fail(HDB_E_INVALID, "min_cluster_size must be >= 2");
+    if (min_samples < 1) return fail(HDB_E_INVALID, "min_samples must be >= 1");
+    if (!(epsilon >= 0) || epsilon > 1.7976931348623157e308)
+        return fail(HDB_E_INVALID, "cluster_selection_epsilon must be finite and >= 0");
+    if (precision == HDB_F32 && epsilon > 3.4028234663852886e38)
+        return fail(HDB_E_INVALID, "cluster_selection_epsilon is not representable in the requested precision");
+    if (offsets_host[0] != 0) return fail(HDB_E_INVALID, "offsets must start at 0");
+    for (int w = 0; w < windows; ++w) {
+        const int64_t n = offsets_host[w + 1] - offsets_host[w];
+        if (n < 2) return fail(HDB_E_INVALID, "X requires nonempty batches/features and at least 2 samples");
+        if (n > HDB_MAX_SAMPLES)
+            return fail(HDB_E_INVALID, "at most " + std::to_string(HDB_MAX_SAMPLES) + " samples per window are supported");
+        if (min_samples > n) return fail(HDB_E_INVALID, "min_samples must not exceed the number of samples");
+    }
+    if (offsets_host[windows] > INT32_MAX) return fail(HDB_E_INVALID, "more than 2^31-1 points in one batch");
+    hdb_plan* p = new hdb_plan();
+    p->precision = precision;
+    p->B = windows;
+    p->D = dims;
+    p->mcs = min_cluster_size;
+    p->ms = min_samples;
+    p->eps = epsilon;
+    p->flags = flags;
+    p->offsets.assign(offsets_host, offsets_host + windows + 1);
+    p->T = offsets_host[windows];
+    p->k = precision == HDB_F32 ? &hdb::kernels_f32() : &hdb::kernels_f64();
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) {
+        delete p;
+        return fail(HDB_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    }
+    int rc = build_plan(p);
+    if (rc) {
+        hdb_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return HDB_OK;
+}
+
+int hdb_plan_destroy(hdb_plan_t* p) {
+    if (!p) return HDB_OK;
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (auto s : p->aux) cudaStreamDestroy(s);
+    for (auto e : p->events) cudaEventDestroy(e);
+    if (p->h_tables) cudaFreeHost(p->h_tables);
+    delete p;
+    return HDB_OK;
+}
+
+size_t hdb_plan_workspace_bytes(const hdb_plan_t* p) { return p ? p->ws_bytes : 0; }
+
+int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
+    if (!p || !buffer || !size) return fail(HDB_E_INVALID, "describe needs a plan and a buffer");
+    std::string s = "{\"precision\":\"" + std::string(p->precision == HDB_F32 ? "float32" : "float64") +
+                    "\",\"windows\":" + std::to_string(p->B) + ",\"points\":" + std::to_string(p->T) +
+                    ",\"dims\":" + std::to_string(p->D) + ",\"workspace_bytes\":" + std::to_string(p->ws_bytes) +
+                    ",\"distance_tiles\":" + std::to_string(p->tiles.size() / 3) + ",\"classes\":[";
+    for (size_t i = 0; i < p->classes.size(); ++i) {
+        const auto& c = p->classes[i];
+        s += (i ? "," : "") + std::string("{\"threads\":") + std::to_string(c.fv->threads) +
+             ",\"vertices_per_thread\":" + std::to_string(c.fv->v) + ",\"register_dims\":" +
+             std::to_string(c.fv->dp) + ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
+             "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"windows\":" +
+             std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
+             std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";
+    }
+    s += "],\"core\":[";
+    for (size_t i = 0; i < p->cores.size(); ++i) {
+        const auto& c = p->cores[i];
+        s += (i ? "," : "") + std::string("{\"kernel\":\"") +
+             (c.cv ? (c.matrix ? "core_matrix" : "core_points") : "core_select") + "\",\"k\":" +
+             std::to_string(c.cv ? c.cv->k : 0) + ",\"register_dims\":" + std::to_string(c.cv ? c.cv->dp : 0) +
+             ",\"items\":" + std::to_string(c.items.size() / 2) + "}";
+    }
+    s += "]}";
+    if (s.size() + 1 > size) return fail(HDB_E_INVALID, "describe buffer too small");
+    std::memcpy(buffer, s.c_str(), s.size() + 1);
+    return HDB_OK;
+}
+
+int hdb_plan_forward(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, size_t ws_bytes, int32_t* status,
+                     const hdb_exports_t* exports, void* stream) {
+    if (!p || !X || !labels) return fail(HDB_E_INVALID, "plan, X and labels are required");
+    int rc = check_device(p);
+    if (rc) return rc;
+    rc = check_workspace(p, ws, ws_bytes);
+    if (rc) return rc;
+    return run_forward(p, X, labels, ws, status, exports, static_cast<cudaStream_t>(stream));
+}
+
+int hdb_plan_capture(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, size_t ws_bytes, int32_t* status,
+                     const hdb_exports_t* exports, void* stream_v) {
+    if (!p || !X || !labels) return fail(HDB_E_INVALID, "plan, X and labels are required");
+    int rc = check_device(p);
+    if (rc) return rc;
+    rc = check_workspace(p, ws, ws_bytes);
+    if (rc) return rc;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+    cudaStream_t capture = stream;
+    bool own = false;
+    if (!capture) {  // the legacy stream cannot be captured
+        HDB_CUDA(cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking));
+        own = true;
+    }
+    HDB_CUDA(cudaStreamBeginCapture(capture, cudaStreamCaptureModeThreadLocal));
+    rc = run_forward(p, X, labels, ws, status, exports, capture);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(capture, &graph);
+    if (own) cudaStreamDestroy(capture);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    p->graph = exec;
+    return HDB_OK;
+}
+
+int hdb_plan_replay(hdb_plan_t* p, void* stream) {
+    if (!p || !p->graph) return fail(HDB_E_INVALID, "plan has no captured graph");
+    int rc = check_device(p);
+    if (rc) return rc;
+    HDB_CUDA(cudaGraphLaunch(p->graph, static_cast<cudaStream_t>(stream)));
+    return HDB_OK;
+}
+
+int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, const void* grad, void* dX, void* ws_v,
+                      size_t ws_bytes, void* stream) {
+    if (!p || !X || !ex || !grad || !dX) return fail(HDB_E_INVALID, "plan, X, exports, grad and dX are required");
+    if (!ex->edges_uv || !ex->order || !ex->link_w)
+        return fail(HDB_E_INVALID, "backward needs the forward's edges_uv, order and link_w");
+    const bool unit = p->ms <= 2;
+    if (!unit && (!ex->core || !ex->core_nbr))
+        return fail(HDB_E_INVALID, "backward with min_samples > 2 needs the forward's core and core_nbr");
+    int rc = check_device(p);
+    if (rc) return rc;
+    rc = check_workspace(p, ws_v, ws_bytes);
+    if (rc) return rc;
+    unsigned char* ws = static_cast<unsigned char*>(ws_v);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    HDB_CUDA(cudaMemcpyAsync(ws, p->h_tables, p->tables_bytes, cudaMemcpyHostToDevice, s));
+    hdb::BackwardArgs a{};
+    a.X = X;
+    a.offsets = reinterpret_cast<const int64_t*>(ws + p->t_offsets);
+    a.edge_window = reinterpret_cast<const int32_t*>(ws + p->t_edge_window);
+    a.n_edges = (int)(p->T - p->B);
+    a.D = p->D;
+    a.unit_core = unit ? 1 : 0;
+    a.edges_uv = ex->edges_uv;
+    a.order = ex->order;
+    a.link_w = ex->link_w;
+    a.grad = grad;
+    a.core = ex->core;
+    a.core_nbr = ex->core_nbr;
+    a.dX = dX;
+    if (a.n_edges > 0) p->k->launch_backward(a, (a.n_edges + 255) / 256, s);
+    HDB_CUDA(cudaGetLastError());
+    return HDB_OK;
+}
+
+size_t hdb_cluster_workspace_bytes(int precision, int batch, int n, int dims, int mcs, int ms) {
+    hdb_plan* p = nullptr;
+    if (cached_plan(precision, batch, n, dims, mcs, ms, 0.0, &p)) return 0;
+    return p->ws_bytes;
+}
+
+int hdb_cluster_f32(const float* X, int batch, int n, int dims, int mcs, int ms, double eps, int32_t* labels,
+                    void* ws, size_t ws_bytes, int32_t* status, void* stream) {
+    return cluster_dense(HDB_F32, X, batch, n, dims, mcs, ms, eps, labels, ws, ws_bytes, status, stream);
+}
+
+int hdb_cluster_f64(const double* X, int batch, int n, int dims, int mcs, int ms, double eps, int32_t* labels,
+                    void* ws, size_t ws_bytes, int32_t* status, void* stream) {
+    return cluster_dense(HDB_F64, X, batch, n, dims, mcs, ms, eps, labels, ws, ws_bytes, status, stream);
+}
+
+}  // extern "C"

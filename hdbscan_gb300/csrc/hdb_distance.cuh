@@ -1,0 +1,332 @@
+// Pairwise distances and self-inclusive core distances.
+//
+// * hdb_distance_kernel: materializes each window's distance block with a
+//   64x64 register-blocked tile per CTA over the upper triangle (tile i <= j)
+//   and writes every off-diagonal tile twice (direct and mirrored), both with
+//   16-byte coalesced stores.  Replaces the one-thread-per-element
+//   DISTANCE_SOURCE (hdbscan_gpu/_kernels.py:45-88) with bit-identical values:
+//   per pair the coordinates are accumulated in k order with
+//   total = total + delta*delta and no FMA, then a correctly rounded sqrt.
+//   Block row stride ld = round_up(n, 4) keeps every row 16-byte aligned.
+// * hdb_core_points_kernel / hdb_core_matrix_kernel: core_i = the (ms-1)-th
+//   smallest distance of row i, self (0) included (reference:
+//   hdbscan_gpu/_cuda.py:114-118, cp.partition).  One thread per row keeps a
+//   sorted register list of the KMAX smallest (value, index) pairs; the value
+//   at position ms-1 is the order statistic, the index is the ms-th nearest
+//   neighbour in (distance, index) order (used by the backward pass).
+// * hdb_core_select_kernel: any ms, one CTA per row, radix select on the
+//   order-preserving bit pattern of the non-negative distances.
+#pragma once
+#include "hdb_common.cuh"
+
+namespace hdb {
+
+__host__ __device__ inline int64_t dist_ld(int n) { return (int64_t)((n + 3) & ~3); }
+
+
+constexpr int kDistTile = 64;
+
+template <typename Real>
+struct DistVec;
+template <> struct DistVec<float> {
+    static constexpr int KC = 32;
+    __device__ static void load4(const float* p, float* out) {
+        const float4 q = *reinterpret_cast<const float4*>(p);
+        out[0] = q.x; out[1] = q.y; out[2] = q.z; out[3] = q.w;
+    }
+    __device__ static void store4(float* p, float a, float b, float c, float d) {
+        *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+    }
+};
+template <> struct DistVec<double> {
+    static constexpr int KC = 16;
+    __device__ static void load4(const double* p, double* out) {
+        const double2 q0 = *reinterpret_cast<const double2*>(p);
+        const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+        out[0] = q0.x; out[1] = q0.y; out[2] = q1.x; out[3] = q1.y;
+    }
+    __device__ static void store4(double* p, double a, double b, double c, double d) {
+        *reinterpret_cast<double2*>(p) = make_double2(a, b);
+        *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
+    }
+};
+
+// 256 threads = 16x16; thread (ty, tx) owns rows ty*4..+3 and cols tx*4..+3.
+template <typename Real>
+__global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs args) {
+    using T = RealTraits<Real>;
+    constexpr int KC = DistVec<Real>::KC;
+    __shared__ __align__(16) Real s_i[KC][kDistTile];
+    __shared__ __align__(16) Real s_j[KC][kDistTile];
+    const int tile = blockIdx.x;
+    if (tile >= args.n_tiles) return;
+    const int w = args.tiles[3 * tile], ti = args.tiles[3 * tile + 1], tj = args.tiles[3 * tile + 2];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const int D = args.D;
+    const Real* __restrict__ Xw = static_cast<const Real*>(args.X) + base * D;
+    Real* __restrict__ Dw = static_cast<Real*>(args.dist) + args.dist_offsets[w];
+    const int64_t ld = dist_ld(n);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int i0 = ti * kDistTile, j0 = tj * kDistTile;
+
+    Real acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = Real(0);
+
+    for (int k0 = 0; k0 < D; k0 += KC) {
+        // Stage [64 rows x KC coords] of each block, transposed to [KC][64].
+        for (int t = tid; t < kDistTile * KC; t += 256) {
+            const int r = t / KC, k = t - r * KC;
+            const int gk = k0 + k;
+            const int gi = i0 + r, gj = j0 + r;
+            s_i[k][r] = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : Real(0);
+            s_j[k][r] = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : Real(0);
+        }
+        __syncthreads();
+        const int kend = min(KC, D - k0);
+        for (int k = 0; k < kend; ++k) {
+            Real xi[4], xj[4];
+            DistVec<Real>::load4(&s_i[k][ty * 4], xi);
+            DistVec<Real>::load4(&s_j[k][tx * 4], xj);
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const Real delta = T::sub(xi[a], xj[b]);
+                    acc[a][b] = T::add(acc[a][b], T::mul(delta, delta));
+                }
+        }
+        __syncthreads();
+    }
+    int overflow = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            acc[a][b] = T::sqrt_rn(acc[a][b]);
+            const int gi = i0 + ty * 4 + a, gj = j0 + tx * 4 + b;
+            if (gi < n && gj < n) overflow |= !(acc[a][b] <= T::kMax);
+        }
+    const int cj = j0 + tx * 4;
+    if (cj < ld) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int gi = i0 + ty * 4 + a;
+            if (gi < n) DistVec<Real>::store4(Dw + gi * ld + cj, acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+        }
+    }
+    if (ti != tj) {
+        const int ci = i0 + ty * 4;
+        if (ci < ld) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int gj = j0 + tx * 4 + b;
+                if (gj < n) DistVec<Real>::store4(Dw + gj * ld + ci, acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
+            }
+        }
+    }
+    if (__syncthreads_or(overflow) && tid == 0) atomic_status(args.status, kOverflow);
+}
+
+// ---------------------------------------------------------------------------
+// Core distances.
+// ---------------------------------------------------------------------------
+
+constexpr int kCoreRows = 128;
+
+// Insert (d, j) into the ascending register list L/LI of length K; strict '<'
+// keeps earlier (smaller) indices ahead among equal values.
+template <typename Real, int K>
+__device__ __forceinline__ void topk_insert(Real (&L)[K], int (&LI)[K], Real d, int j) {
+    if (!(d < L[K - 1])) return;
+#pragma unroll
+    for (int t = K - 1; t > 0; --t) {
+        if (d < L[t - 1]) { L[t] = L[t - 1]; LI[t] = LI[t - 1]; }
+        else if (d < L[t]) { L[t] = d; LI[t] = j; }
+    }
+    if (d < L[0]) { L[0] = d; LI[0] = j; }
+}
+
+template <typename Real, int K>
+__device__ __forceinline__ void topk_pick(const Real (&L)[K], const int (&LI)[K], int k, Real& value, int& index) {
+#pragma unroll
+    for (int t = 0; t < K; ++t)
+        if (t == k) { value = L[t]; index = LI[t]; }
+}
+
+// Rows from points: 128 rows per CTA, j tiles staged in shared memory.
+template <typename Real, int K, int DP>
+__global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreArgs args) {
+    using T = RealTraits<Real>;
+    constexpr int TJ = 64;
+    constexpr int VEC = 16 / (int)sizeof(Real);
+    static_assert(DP % VEC == 0, "DP must be a multiple of one 16-byte vector");
+    __shared__ __align__(16) Real s_x[TJ * DP];
+    const int item = blockIdx.x;
+    if (item >= args.n_items) return;
+    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const int D = args.D;
+    const Real* __restrict__ Xw = static_cast<const Real*>(args.X) + base * D;
+    const int i = r0 + threadIdx.x;
+    Real xi[DP];
+#pragma unroll
+    for (int k = 0; k < DP; ++k) xi[k] = (i < n && k < D) ? Xw[(int64_t)i * D + k] : Real(0);
+    Real L[K];
+    int LI[K];
+#pragma unroll
+    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
+    int overflow = 0;
+    for (int j0 = 0; j0 < n; j0 += TJ) {
+        const int cnt = min(TJ, n - j0);
+        for (int t = threadIdx.x; t < TJ * DP; t += kCoreRows) {
+            const int r = t / DP, k = t - r * DP;
+            s_x[t] = (r < cnt && k < D) ? Xw[(int64_t)(j0 + r) * D + k] : Real(0);
+        }
+        __syncthreads();
+        if (i < n) {
+            for (int jj = 0; jj < cnt; ++jj) {
+                Real acc = Real(0);
+#pragma unroll
+                for (int k0 = 0; k0 < DP; k0 += VEC) {
+                    Real c[VEC];
+                    if constexpr (sizeof(Real) == 4) {
+                        const float4 q = *reinterpret_cast<const float4*>(&s_x[jj * DP + k0]);
+                        c[0] = q.x; c[1 % VEC] = q.y; c[2 % VEC] = q.z; c[3 % VEC] = q.w;
+                    } else {
+                        const double2 q = *reinterpret_cast<const double2*>(&s_x[jj * DP + k0]);
+                        c[0] = q.x; c[1 % VEC] = q.y;
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < VEC; ++kk) {
+                        const Real delta = T::sub(xi[k0 + kk], c[kk]);
+                        acc = T::add(acc, T::mul(delta, delta));
+                    }
+                }
+                const Real d = T::sqrt_rn(acc);
+                overflow |= !(d <= T::kMax);
+                topk_insert<Real, K>(L, LI, d, j0 + jj);
+            }
+        }
+        __syncthreads();
+    }
+    if (i < n) {
+        Real value = Real(0);
+        int index = -1;
+        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = value;
+        if (args.core_nbr) args.core_nbr[base + i] = index;
+    }
+    if (__syncthreads_or(overflow) && threadIdx.x == 0) atomic_status(args.status, kOverflow);
+}
+
+// Rows from the materialized matrix: thread i reads column i (the block is
+// symmetric), so every step is one coalesced row segment.
+template <typename Real, int K>
+__global__ void __launch_bounds__(kCoreRows) hdb_core_matrix_kernel(const CoreArgs args) {
+    using T = RealTraits<Real>;
+    const int item = blockIdx.x;
+    if (item >= args.n_items) return;
+    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const Real* __restrict__ Dw = static_cast<const Real*>(args.dist) + args.dist_offsets[w];
+    const int64_t ld = dist_ld(n);
+    const int i = r0 + threadIdx.x;
+    if (i >= n) return;
+    Real L[K];
+    int LI[K];
+#pragma unroll
+    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
+    for (int j = 0; j < n; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + j * ld + i), j);
+    Real value = Real(0);
+    int index = -1;
+    topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
+    static_cast<Real*>(args.core)[base + i] = value;
+    if (args.core_nbr) args.core_nbr[base + i] = index;
+}
+
+// Any ms: one CTA (256 threads) per row; the row is computed (or read) into
+// shared memory, then a most-significant-digit radix select over 8-bit digits
+// of the order-preserving key finds the (ms-1)-th value; the neighbour index
+// is the position's element in (value, index) order.
+template <typename Real>
+__global__ void __launch_bounds__(256) hdb_core_select_kernel(const CoreArgs args) {
+    using T = RealTraits<Real>;
+    using Key = typename T::Bits;
+    constexpr int kBits = 8 * (int)sizeof(Key);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Key* s_key = reinterpret_cast<Key*>(smem_raw);
+    __shared__ int s_hist[256];
+    __shared__ int s_pick[2];
+    __shared__ int s_overflow;
+    const int row = blockIdx.x;
+    // items here are (window, row) pairs, one per CTA.
+    if (row >= args.n_items) return;
+    const int w = args.items[2 * row], i = args.items[2 * row + 1];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const int D = args.D;
+    if (threadIdx.x == 0) s_overflow = 0;
+    __syncthreads();
+    int overflow = 0;
+    if (args.dist) {
+        const Real* Dw = static_cast<const Real*>(args.dist) + args.dist_offsets[w] + i * dist_ld(n);
+        for (int j = threadIdx.x; j < n; j += 256) s_key[j] = T::key(Dw[j]);
+    } else {
+        const Real* Xw = static_cast<const Real*>(args.X) + base * D;
+        for (int j = threadIdx.x; j < n; j += 256) {
+            Real acc = Real(0);
+            for (int k = 0; k < D; ++k) {
+                const Real delta = T::sub(Xw[(int64_t)i * D + k], Xw[(int64_t)j * D + k]);
+                acc = T::add(acc, T::mul(delta, delta));
+            }
+            const Real d = T::sqrt_rn(acc);
+            overflow |= !(d <= T::kMax);
+            s_key[j] = T::key(d);
+        }
+    }
+    if (overflow) atomicOr(&s_overflow, 1);
+    __syncthreads();
+    int k = args.ms - 1;          // rank still to skip inside the current prefix
+    Key prefix = 0, mask = 0;
+    for (int shift = kBits - 8; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += 256) s_hist[b] = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += 256)
+            if ((s_key[j] & mask) == prefix) atomicAdd(&s_hist[(s_key[j] >> shift) & 0xff], 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0, b = 0;
+            for (; b < 256; ++b) {
+                if (acc + s_hist[b] > k) break;
+                acc += s_hist[b];
+            }
+            s_pick[0] = b;
+            s_pick[1] = acc;
+        }
+        __syncthreads();
+        prefix |= (Key)s_pick[0] << shift;
+        mask |= (Key)0xff << shift;
+        k -= s_pick[1];
+        __syncthreads();
+    }
+    // prefix is the value; k elements equal to it come before the chosen one.
+    if (threadIdx.x == 0) {
+        int seen = 0, index = -1;
+        for (int j = 0; j < n; ++j)
+            if (s_key[j] == prefix) {
+                if (seen == k) { index = j; break; }
+                ++seen;
+            }
+        static_cast<Real*>(args.core)[base + i] = T::from_key(prefix);
+        if (args.core_nbr) args.core_nbr[base + i] = index;
+        if (s_overflow) atomic_status(args.status, kOverflow);
+    }
+}
+
+}  // namespace hdb

@@ -1,0 +1,38 @@
+// float64 kernel variants.  Register budget: V*DP doubles of coordinates per
+// thread stay <= 16 at 1024 threads and <= 32 below.
+#include "hdb_instances.cuh"
+
+namespace hdb {
+namespace {
+const ForwardVariant kForward[] = {
+    forward_variant<double, 128, 1, 8>(),  forward_variant<double, 128, 1, 16>(),
+    forward_variant<double, 128, 1, 0>(),
+    forward_variant<double, 256, 1, 8>(),  forward_variant<double, 256, 1, 16>(),
+    forward_variant<double, 256, 1, 0>(),
+    forward_variant<double, 512, 1, 8>(),  forward_variant<double, 512, 1, 16>(),
+    forward_variant<double, 512, 1, 0>(),
+    forward_variant<double, 512, 2, 8>(),  forward_variant<double, 512, 2, 16>(),
+    forward_variant<double, 512, 2, 0>(),
+    forward_variant<double, 1024, 2, 8>(), forward_variant<double, 1024, 2, 0>(),
+    forward_variant<double, 1024, 4, 0>(),
+};
+const CoreVariant kCore[] = {
+    core_points_variant<double, 8, 8>(),   core_points_variant<double, 8, 16>(),
+    core_points_variant<double, 8, 32>(),
+    core_points_variant<double, 16, 8>(),  core_points_variant<double, 16, 16>(),
+    core_points_variant<double, 16, 32>(),
+    core_points_variant<double, 32, 8>(),  core_points_variant<double, 32, 16>(),
+    core_points_variant<double, 32, 32>(),
+    core_points_variant<double, 64, 8>(),  core_points_variant<double, 64, 16>(),
+    core_points_variant<double, 64, 32>(),
+    core_matrix_variant<double, 8>(),      core_matrix_variant<double, 16>(),
+    core_matrix_variant<double, 32>(),     core_matrix_variant<double, 64>(),
+};
+const PrecisionKernels kTable = {
+    8, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), kCore, (int)(sizeof(kCore) / sizeof(kCore[0])),
+    launch_distance<double>, launch_select<double>, (const void*)hdb_core_select_kernel<double>,
+    launch_backward<double>, forward_smem_dispatch<double>,
+};
+}  // namespace
+const PrecisionKernels& kernels_f64() { return kTable; }
+}  // namespace hdb

@@ -1,0 +1,142 @@
+/*
+ * hdbscan_gb300 — C ABI of the GB300 (sm_103a) batched HDBSCAN library.
+ *
+ * Drop-in for the CUDA path of CosineAI/hdbscan's
+ *   hdbscan_gpu.hdbscan(X, backend="cuda", precision=..., min_cluster_size,
+ *                       min_samples, cluster_selection_epsilon) -> int32 labels
+ * whose backend seam is `cluster(x, min_cluster_size, min_samples, epsilon,
+ * precision)` (hdbscan_gpu/_api.py:92-102, implemented by
+ * hdbscan_gpu/_cuda.py:91-128).
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success or a negative HDB_E_* code; the
+ *    message of the calling thread's last failure is hdb_last_error().  No C++
+ *    exception crosses this boundary.
+ *  - Device pointers are plain addresses on the device that was current when
+ *    the plan was created; `stream` is a cudaStream_t (NULL = legacy default).
+ *    All device work is ordered on `stream`; nothing synchronizes the host.
+ *  - The library allocates no device memory per call: the caller passes a
+ *    workspace of hdb_plan_workspace_bytes() bytes (256-byte aligned).
+ *  - Results are bit-exact with the reference CUDA path: Prim edges, NumPy
+ *    tie order of the edge sort, linkage ids/orientation/weights/sizes,
+ *    condensed clusters and labels.
+ *  - The device status word is a bit-or of HDB_STATUS_*; it is zeroed by each
+ *    forward call and read by the caller after synchronizing (the reference
+ *    raises at its two host syncs, _cuda.py:98-99 and :112-113).
+ */
+#ifndef HDBSCAN_GB300_H
+#define HDBSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HDB_VERSION 1
+
+#define HDB_F32 0
+#define HDB_F64 1
+
+#define HDB_MAX_SAMPLES 4096 /* points per window, as MAX_SAMPLES at hdbscan_gpu/_api.py:7 */
+
+/* Return codes. */
+#define HDB_OK 0
+#define HDB_E_INVALID (-1)   /* bad argument (message says which) */
+#define HDB_E_CUDA (-2)      /* a CUDA runtime call failed */
+#define HDB_E_WORKSPACE (-3) /* workspace missing, too small or misaligned */
+#define HDB_E_DEVICE (-4)    /* called with a different current device than the plan's */
+
+/* Device status bits (bit-or). */
+#define HDB_STATUS_OVERFLOW 1  /* a pairwise distance overflowed the precision */
+#define HDB_STATUS_NONFINITE 2 /* an input coordinate is NaN or infinite (outranks overflow) */
+#define HDB_STATUS_INTERNAL 4  /* a device-side consistency check failed */
+
+/* Plan flags. */
+#define HDB_FLAG_FORCE_MATRIX 1u /* materialize every window's distance block (matrix Prim) */
+#define HDB_FLAG_NO_GRAPH_STREAMS 2u /* run all window classes on the caller's stream */
+
+typedef struct hdb_plan hdb_plan_t;
+
+/* Optional device outputs of a forward call; NULL members are skipped.
+ * E = sum over windows of (n_w - 1) edges; T = sum of n_w points; B windows.
+ * Edge rows of window w start at offsets[w] - w, per-point and per-cluster
+ * rows at offsets[w] (clusters are indexed by condensed id - n_w). */
+typedef struct hdb_exports {
+    int32_t* edges_uv;     /* [E,2] Prim edges (source, new vertex), window-local ids */
+    void* edge_w;          /* [E]   Prim edge weights (Real) */
+    int32_t* order;        /* [E]   NumPy-quicksort order of edge_w (window-local) */
+    int32_t* link_lr;      /* [E,2] single-linkage children of node n_w + i */
+    void* link_w;          /* [E]   merge weights (Real), sklearn single_linkage_tree_ 'value' */
+    int32_t* link_size;    /* [E]   merged cluster sizes */
+    int32_t* n_clusters;   /* [B]   condensed clusters incl. the root */
+    int32_t* cl_parent;    /* [T]   condensed parent id (-1 for the root) */
+    void* cl_birth;        /* [T]   lambda at which the cluster was born (Real) */
+    void* cl_stability;    /* [T]   stability after excess-of-mass selection (Real) */
+    uint8_t* cl_selected;  /* [T]   final selection flag */
+    int32_t* point_parent; /* [T]   condensed cluster each point falls out of */
+    void* core;            /* [T]   core distances (Real); written when min_samples > 2 */
+    int32_t* core_nbr;     /* [T]   ms-th nearest neighbour in (distance, index) order */
+} hdb_exports_t;
+
+/* Library version (HDB_VERSION). */
+int hdb_version(void);
+
+/* Message of the calling thread's most recent failure ("" if none). */
+const char* hdb_last_error(void);
+
+/* Build a plan for a ragged batch: `windows` windows whose points are rows
+ * offsets_host[w] .. offsets_host[w+1]-1 of a packed [T, dims] array.
+ * Validation and messages follow hdbscan_gpu/_api.py:32-87: min_cluster_size
+ * >= 2, 1 <= min_samples <= every n_w, 2 <= n_w <= HDB_MAX_SAMPLES.  The plan
+ * chooses per-window kernel variants (autotune table), sorts windows by size
+ * into a persistent work queue and owns a pinned copy of its device tables.
+ * Replaces the per-call kernel selection of hdbscan_gpu/_cuda.py:66-88. */
+int hdb_plan_create(hdb_plan_t** plan, int precision, int windows, const int64_t* offsets_host, int dims,
+                    int min_cluster_size, int min_samples, double epsilon, unsigned flags);
+
+int hdb_plan_destroy(hdb_plan_t* plan);
+
+/* Bytes of device workspace a forward/backward call of this plan needs. */
+size_t hdb_plan_workspace_bytes(const hdb_plan_t* plan);
+
+/* JSON description of the plan's window classes and kernel choices. */
+int hdb_plan_describe(const hdb_plan_t* plan, char* buffer, size_t size);
+
+/* Cluster the batch: X is the packed [T, dims] Real array, labels [T] int32
+ * (-1 noise), status one int32.  Replaces hdbscan_gpu/_cuda.py:91-128. */
+int hdb_plan_forward(hdb_plan_t* plan, const void* X, int32_t* labels, void* workspace, size_t workspace_bytes,
+                     int32_t* status, const hdb_exports_t* exports, void* stream);
+
+/* Capture hdb_plan_forward with these exact pointers into a CUDA graph owned
+ * by the plan (replacing any previous one), then hdb_plan_replay() launches
+ * it.  The pointers must stay valid while the graph is used. */
+int hdb_plan_capture(hdb_plan_t* plan, const void* X, int32_t* labels, void* workspace, size_t workspace_bytes,
+                     int32_t* status, const hdb_exports_t* exports, void* stream);
+int hdb_plan_replay(hdb_plan_t* plan, void* stream);
+
+/* Gradient of the merge weights with respect to X (no reference
+ * counterpart: the reference has no gradients).  `exports` must hold the
+ * edges_uv, order and link_w of the forward call on the same X (and core,
+ * core_nbr when min_samples > 2); grad is [E] Real in linkage order; dX is
+ * [T, dims] Real and is accumulated into (zero it first). */
+int hdb_plan_backward(hdb_plan_t* plan, const void* X, const hdb_exports_t* exports, const void* grad, void* dX,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* Dense uniform batch, the reference seam itself: X [batch, n, dims]
+ * contiguous, labels [batch, n].  Plans are cached per shape/parameters. */
+size_t hdb_cluster_workspace_bytes(int precision, int batch, int n, int dims, int min_cluster_size,
+                                   int min_samples);
+int hdb_cluster_f32(const float* X, int batch, int n, int dims, int min_cluster_size, int min_samples,
+                    double epsilon, int32_t* labels, void* workspace, size_t workspace_bytes, int32_t* status,
+                    void* stream);
+int hdb_cluster_f64(const double* X, int batch, int n, int dims, int min_cluster_size, int min_samples,
+                    double epsilon, int32_t* labels, void* workspace, size_t workspace_bytes, int32_t* status,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HDBSCAN_GB300_H */
