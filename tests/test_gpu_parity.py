@@ -89,9 +89,17 @@ def test_small_ragged_batch_matches_oracle(cuda, precision, mcs, ms, eps):
 def test_size_classes_match_oracle(cuda, precision, force_matrix):
     # One window per size class boundary (128/256/512/1024/2048/4096).
     rng = np.random.default_rng(7)
-    sizes = [2, 3, 128, 129, 256, 257, 512, 513, 1024, 1025, 2048, 2049]
+    sizes = [4, 5, 128, 129, 256, 257, 512, 513, 1024, 1025, 2048, 2049]
     windows = [rng.normal(size=(n, 5)) for n in sizes]
     _compare(windows, 5, 4, 0.1, precision, force_matrix)
+
+
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+@pytest.mark.parametrize("ms", [1, 2])
+def test_two_and_three_point_windows(cuda, precision, ms):
+    rng = np.random.default_rng(ms)
+    windows = [rng.normal(size=(n, 2)) for n in (2, 3, 2, 3, 4)]
+    _compare(windows, 2, ms, 0.1, precision)
 
 
 @pytest.mark.parametrize("precision", ["float32", "float64"])
