@@ -90,6 +90,19 @@ namespace {
 
 int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
 
+// The dynamic shared-memory limit is a per-function attribute shared by every
+// plan in the process, so it only ever grows: lowering it to one plan's need
+// would break launches of an earlier plan with larger windows.
+std::mutex g_attr_mutex;
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, func);
+    if (e != cudaSuccess) return e;
+    if ((size_t)attr.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // Autotune table: (threads, vertices per thread) by window size, register
 // dimensions by D.  Windows whose coordinates do not fit the register budget
 // of an instantiated variant use the matrix variant.
@@ -242,16 +255,14 @@ int build_plan(hdb_plan* p) {
     // ---- grids --------------------------------------------------------------
     for (auto& c : p->classes) {
         c.smem = k.forward_smem(c.nmax, c.fv->dp, c.x_in_smem, unit);
-        HDB_CUDA(cudaFuncSetAttribute(c.fv->func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
+        HDB_CUDA(raise_smem_limit(c.fv->func, c.smem));
         int per_sm = 0;
         HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads, c.smem));
         if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
         c.grid = (int)std::min<size_t>(c.windows.size(), (size_t)per_sm * p->sms);
     }
     for (auto& c : p->cores)
-        if (!c.cv && c.select_smem > 48 * 1024)
-            HDB_CUDA(cudaFuncSetAttribute(k.select_func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)c.select_smem));
+        if (!c.cv && c.select_smem > 48 * 1024) HDB_CUDA(raise_smem_limit(k.select_func, c.select_smem));
 
     // ---- table image --------------------------------------------------------
     std::vector<unsigned char> image;
