@@ -180,6 +180,8 @@ def main():
     parser.add_argument("--cpu-windows", type=int, default=256)
     parser.add_argument("--plain-passes", type=int, default=2)
     parser.add_argument("--skip-cpu", action="store_true")
+    parser.add_argument("--profile", action="store_true",
+                        help="only warm-up + timed graph replays (for ncu captures); prints nothing else")
     args = parser.parse_args()
     if args.warmup < 3:
         parser.error("--warmup must be >= 3")
@@ -246,6 +248,9 @@ def main():
             end.synchronize()
             step_ms.append(start.elapsed_time(end))
     torch.cuda.synchronize()
+    if args.profile:
+        print(json.dumps({"profile_ms_per_step": float(np.mean(step_ms))}))
+        return
     ms_per_step = float(np.mean(step_ms))
     if world > 1:
         t = torch.tensor([ms_per_step], device=device)

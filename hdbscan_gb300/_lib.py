@@ -55,6 +55,8 @@ def _declare(handle):
                                                                         _P, _P]),
         "hdb_cluster_f64": (ctypes.c_int, [_P] + [ctypes.c_int] * 5 + [ctypes.c_double, _P, _P, ctypes.c_size_t,
                                                                         _P, _P]),
+        "hdb_cluster_noalloc": (ctypes.c_int, [ctypes.c_int, _P] + [ctypes.c_int] * 5 + [ctypes.c_double, _P, _P,
+                                                                                          _P]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(handle, name)
@@ -66,7 +68,7 @@ def _declare(handle):
 # Every symbol include/hdbscan_gb300.h declares.
 SYMBOLS = ("hdb_version", "hdb_last_error", "hdb_plan_create", "hdb_plan_destroy", "hdb_plan_workspace_bytes",
            "hdb_plan_describe", "hdb_plan_forward", "hdb_plan_capture", "hdb_plan_replay", "hdb_plan_backward",
-           "hdb_cluster_workspace_bytes", "hdb_cluster_f32", "hdb_cluster_f64")
+           "hdb_cluster_workspace_bytes", "hdb_cluster_f32", "hdb_cluster_f64", "hdb_cluster_noalloc")
 
 
 def lib():

@@ -86,15 +86,15 @@ struct hdb_plan {
     cudaGraphExec_t graph = nullptr;
 };
 
-namespace {
+namespace hdb {
 
-int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
+void set_last_error(const char* message) { g_error = message; }
 
 // The dynamic shared-memory limit is a per-function attribute shared by every
-// plan in the process, so it only ever grows: lowering it to one plan's need
+// caller in the process, so it only ever grows: lowering it to one plan's need
 // would break launches of an earlier plan with larger windows.
-std::mutex g_attr_mutex;
-cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+static std::mutex g_attr_mutex;
+cudaError_t raise_dynamic_smem(const void* func, size_t bytes) {
     std::lock_guard<std::mutex> lock(g_attr_mutex);
     cudaFuncAttributes attr;
     cudaError_t e = cudaFuncGetAttributes(&attr, func);
@@ -102,6 +102,14 @@ cudaError_t raise_smem_limit(const void* func, size_t bytes) {
     if ((size_t)attr.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
     return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
+
+}  // namespace hdb
+
+namespace {
+
+int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
+
+cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise_dynamic_smem(func, bytes); }
 
 // Autotune table: (threads, vertices per thread) by window size, register
 // dimensions by D.  Windows whose coordinates do not fit the register budget

@@ -1,0 +1,230 @@
+// Dense-batch forward that allocates nothing (hdb_cluster_noalloc).
+//
+// Who needs it: a caller that may not call cudaMalloc at the point where it
+// clusters -- for example a serving process that hands all device memory to
+// its own pool at start-up and treats any other allocation as a failure, or a
+// plugin living inside a host framework whose allocator owns the device.  Such
+// a caller can still pass its input and output buffers, but cannot provide the
+// workspace the planned entry points ask for.
+//
+// How: the forward kernel's scratch (window offsets, work queue, queue ticket,
+// core-distance work items, core distances) lives in one file-scope
+// __device__ array of kScratchBytes, resident on every device that loads this
+// library until the process exits.  Host code must not use the array's name as
+// a device address (in host code it names a host-side stand-in), so the first
+// call on each device resolves the real address once with
+// cudaGetSymbolAddress, with that device current, and caches it.  That first
+// call should therefore come before any stream capture.  A small kernel
+// rebuilds the tables in the scratch on every call (nothing is copied from
+// host memory), so no pinned buffer is needed either.
+//
+// Every call shares the array and overwrites what the previous call left:
+// calls that overlap on the GPU (other streams, other host threads) race with
+// each other; keep them ordered on one stream.
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hdbscan_gb300.h"
+#include "hdb_args.h"
+#include "hdb_registry.h"
+
+namespace {
+
+constexpr size_t kScratchBytes = HDB_NOALLOC_SCRATCH_BYTES;
+constexpr int kMaxDevices = 64;
+
+// Byte layout of the scratch array.
+constexpr size_t kOffOffsets = 0;                                                     // int64 [windows+1]
+constexpr size_t kOffQueue = (((size_t)(HDB_NOALLOC_MAX_WINDOWS + 1) * 8 + 255) / 256) * 256;  // int32 [windows]
+constexpr size_t kOffTicket = kOffQueue + (((size_t)HDB_NOALLOC_MAX_WINDOWS * 4 + 255) / 256) * 256;
+constexpr size_t kOffItems = kOffTicket + 256;                                        // int32 [2*points]
+constexpr size_t kOffCore = kOffItems + (size_t)HDB_NOALLOC_MAX_POINTS * 8;          // Real [points]
+constexpr size_t kScratchUsed = kOffCore + (size_t)HDB_NOALLOC_MAX_POINTS * 8;
+static_assert(kScratchUsed <= kScratchBytes, "no-allocation scratch layout exceeds its array");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_scratch_mutex;
+unsigned char* g_scratch_device[kMaxDevices] = {};
+
+// Failures are reported through the library's hdb_last_error().
+int fail(int code, const std::string& message) {
+    hdb::set_last_error(message);
+    return code;
+}
+
+// Device address of the scratch array on `device` (which must be current).
+int scratch_address(int device, unsigned char** out) {
+    if (device < 0 || device >= kMaxDevices) return fail(HDB_E_DEVICE, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_device[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(HDB_E_CUDA, std::string("cudaGetSymbolAddress(no-allocation scratch): ") +
+                                        cudaGetErrorString(e));
+        g_scratch_device[device] = static_cast<unsigned char*>(ptr);
+    }
+    *out = g_scratch_device[device];
+    return HDB_OK;
+}
+
+// Rebuilds the uniform-batch tables; also zeroes the ticket and the status.
+__global__ void noalloc_tables_kernel(int64_t* offsets, int32_t* queue, int32_t* ticket, int32_t* items, int batch,
+                                      int n, int rows_per_item, int n_items, int32_t* status) {
+    const int stride = gridDim.x * blockDim.x;
+    const int per_window = (n + rows_per_item - 1) / rows_per_item;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < batch + 1 || t < n_items; t += stride) {
+        if (t <= batch) offsets[t] = (int64_t)t * n;
+        if (t < batch) queue[t] = t;
+        if (t < n_items) {
+            const int w = t / per_window;
+            items[2 * t] = w;
+            items[2 * t + 1] = (t - w * per_window) * rows_per_item;
+        }
+        if (t == 0) {
+            ticket[0] = 0;
+            if (status) status[0] = 0;
+        }
+    }
+}
+
+const hdb::ForwardVariant* pick_forward(const hdb::PrecisionKernels& k, int precision, int n, int dims) {
+    int threads, v;
+    if (n <= 128) { threads = 128; v = 1; }
+    else if (n <= 256) { threads = 256; v = 1; }
+    else if (n <= 512) { threads = 512; v = 1; }
+    else if (n <= 1024) { threads = 512; v = 2; }
+    else if (n <= 2048) { threads = 1024; v = 2; }
+    else { threads = 1024; v = 4; }
+    for (int dp : {8, 16, 32}) {
+        if (dims > dp || (precision == HDB_F64 && dp > 16)) continue;
+        for (int i = 0; i < k.n_forward; ++i)
+            if (k.forward[i].threads == threads && k.forward[i].v == v && k.forward[i].dp == dp) return &k.forward[i];
+    }
+    return nullptr;
+}
+
+const hdb::CoreVariant* pick_core(const hdb::PrecisionKernels& k, int precision, int ms, int dims) {
+    for (int K : {8, 16, 32, 64}) {
+        if (ms > K) continue;
+        for (int dp : {8, 16, 32, 64}) {
+            if (dims > dp || (precision == HDB_F64 && dp > 32)) continue;
+            for (int i = 0; i < k.n_core; ++i)
+                if (k.core[i].k == K && k.core[i].dp == dp) return &k.core[i];
+        }
+        return nullptr;
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int n, int dims, int min_cluster_size,
+                                   int min_samples, double epsilon, int32_t* labels, int32_t* status, void* stream_v) {
+    if (precision != HDB_F32 && precision != HDB_F64)
+        return fail(HDB_E_INVALID, "precision must be 'float32' or 'float64'");
+    if (!X || !labels) return fail(HDB_E_INVALID, "X and labels are required");
+    if (batch < 1 || dims < 1 || n < 2)
+        return fail(HDB_E_INVALID, "X requires nonempty batches/features and at least 2 samples");
+    if (n > HDB_MAX_SAMPLES) return fail(HDB_E_INVALID, "at most 4096 samples per window are supported");
+    if (min_cluster_size < 2) return fail(HDB_E_INVALID, "min_cluster_size must be >= 2");
+    if (min_samples < 1) return fail(HDB_E_INVALID, "min_samples must be >= 1");
+    if (min_samples > n) return fail(HDB_E_INVALID, "min_samples must not exceed the number of samples");
+    if (!(epsilon >= 0) || epsilon > 1.7976931348623157e308)
+        return fail(HDB_E_INVALID, "cluster_selection_epsilon must be finite and >= 0");
+    if (batch > HDB_NOALLOC_MAX_WINDOWS || (int64_t)batch * n > HDB_NOALLOC_MAX_POINTS)
+        return fail(HDB_E_INVALID, "batch of " + std::to_string(batch) + " x " + std::to_string(n) +
+                                       " points exceeds the no-allocation limit (at most " +
+                                       std::to_string(HDB_NOALLOC_MAX_WINDOWS) + " windows and " +
+                                       std::to_string(HDB_NOALLOC_MAX_POINTS) + " points)");
+    const int max_dims = precision == HDB_F32 ? 32 : 16;
+    if (dims > max_dims)
+        return fail(HDB_E_INVALID, "dims above " + std::to_string(max_dims) +
+                                       " need the distance-block workspace of hdb_plan_*; the no-allocation "
+                                       "entry point keeps no room for it");
+
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    unsigned char* scratch = nullptr;
+    int rc = scratch_address(device, &scratch);
+    if (rc) return rc;
+
+    const hdb::PrecisionKernels& k = precision == HDB_F32 ? hdb::kernels_f32() : hdb::kernels_f64();
+    const bool unit = min_samples <= 2;
+    const hdb::ForwardVariant* fv = pick_forward(k, precision, n, dims);
+    if (!fv) return fail(HDB_E_INVALID, "no register variant for this window size and dims");
+    const hdb::CoreVariant* cv = unit ? nullptr : pick_core(k, precision, min_samples, dims);
+
+    int optin = 0, sms = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+    int xs = 1;
+    size_t smem = k.forward_smem(n, fv->dp, true, unit);
+    if (smem > (size_t)optin - 2048) { xs = 0; smem = k.forward_smem(n, fv->dp, false, unit); }
+    e = hdb::raise_dynamic_smem(fv->func, smem);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fv->func, fv->threads, smem);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("forward kernel set-up: ") + cudaGetErrorString(e));
+    if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
+    const size_t select_smem = (size_t)n * (precision == HDB_F32 ? 4 : 8);
+    if (!unit && !cv && select_smem > 48 * 1024) {
+        e = hdb::raise_dynamic_smem(k.select_func, select_smem);
+        if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("select kernel set-up: ") + cudaGetErrorString(e));
+    }
+
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+    int64_t* offsets = reinterpret_cast<int64_t*>(scratch + kOffOffsets);
+    int32_t* queue = reinterpret_cast<int32_t*>(scratch + kOffQueue);
+    int32_t* ticket = reinterpret_cast<int32_t*>(scratch + kOffTicket);
+    int32_t* items = reinterpret_cast<int32_t*>(scratch + kOffItems);
+    void* core = scratch + kOffCore;
+    const int rows_per_item = unit ? 1 : (cv ? 128 : 1);
+    const int n_items = unit ? 0 : batch * ((n + rows_per_item - 1) / rows_per_item);
+    const int work = (batch + 1 > n_items ? batch + 1 : n_items);
+    noalloc_tables_kernel<<<(work + 255) / 256, 256, 0, stream>>>(offsets, queue, ticket, items, batch, n,
+                                                                   rows_per_item, n_items, status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("tables kernel: ") + cudaGetErrorString(e));
+
+    if (!unit) {
+        hdb::CoreArgs a{};
+        a.X = X;
+        a.offsets = offsets;
+        a.items = items;
+        a.n_items = n_items;
+        a.D = dims;
+        a.ms = min_samples;
+        a.core = core;
+        a.status = status;
+        if (cv) cv->launch(a, n_items, stream);
+        else k.launch_select(a, n_items, select_smem, stream);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("core kernel: ") + cudaGetErrorString(e));
+    }
+
+    hdb::ForwardArgs a{};
+    a.X = X;
+    a.offsets = offsets;
+    a.queue = queue;
+    a.queue_len = batch;
+    a.ticket = ticket;
+    a.D = dims;
+    a.mcs = min_cluster_size;
+    a.unit_core = unit ? 1 : 0;
+    a.x_in_smem = xs;
+    a.eps = epsilon;
+    a.core = unit ? nullptr : core;
+    a.labels = labels;
+    a.status = status;
+    const int grid = batch < per_sm * sms ? batch : per_sm * sms;
+    fv->launch(a, grid, smem, stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("forward kernel: ") + cudaGetErrorString(e));
+    return HDB_OK;
+}

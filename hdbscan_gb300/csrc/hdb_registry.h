@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "hdb_args.h"
@@ -38,5 +39,12 @@ struct PrecisionKernels {
 
 const PrecisionKernels& kernels_f32();
 const PrecisionKernels& kernels_f64();
+
+// Raise (never lower) a kernel's dynamic shared-memory limit; thread-safe.
+cudaError_t raise_dynamic_smem(const void* func, size_t bytes);
+
+// Message returned by hdb_last_error() on the calling thread.
+void set_last_error(const char* message);
+inline void set_last_error(const std::string& message) { set_last_error(message.c_str()); }
 
 }  // namespace hdb

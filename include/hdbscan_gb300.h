@@ -135,6 +135,29 @@ int hdb_cluster_f64(const double* X, int batch, int n, int dims, int min_cluster
                     double epsilon, int32_t* labels, void* workspace, size_t workspace_bytes, int32_t* status,
                     void* stream);
 
+/* Dense batch without any device allocation.  This entry point has no
+ * counterpart in the reference.  It serves callers that may not allocate
+ * device memory where they cluster: a serving process that gives all device
+ * memory to its own pool at start-up and treats any other allocation as an
+ * error, or a plugin whose host framework owns the device allocator.  They
+ * pass X and labels (and status) as usual; the scratch the kernels need
+ * (window tables, work queue, core distances) is one array of
+ * HDB_NOALLOC_SCRATCH_BYTES compiled into this library, which stays resident
+ * on every device that loads the library until the process exits.
+ *  - Limits: batch <= HDB_NOALLOC_MAX_WINDOWS, batch*n <= HDB_NOALLOC_MAX_POINTS,
+ *    dims <= 32 (float32) / 16 (float64); larger requests fail with
+ *    HDB_E_INVALID and a message naming the limit.
+ *  - The first call on a device looks up the array's device address with that
+ *    device current; make that first call before any stream capture.
+ *  - All calls share the one array and overwrite it: calls that overlap on the
+ *    GPU (other streams or host threads) race; order them on one stream.
+ *  - Calls no cudaMalloc/cudaFree and no allocating library routine. */
+#define HDB_NOALLOC_MAX_WINDOWS 16384
+#define HDB_NOALLOC_MAX_POINTS 262144
+#define HDB_NOALLOC_SCRATCH_BYTES (5u << 20)
+int hdb_cluster_noalloc(int precision, const void* X, int batch, int n, int dims, int min_cluster_size,
+                        int min_samples, double epsilon, int32_t* labels, int32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
