@@ -180,6 +180,7 @@ def main():
     parser.add_argument("--cpu-windows", type=int, default=256)
     parser.add_argument("--plain-passes", type=int, default=2)
     parser.add_argument("--skip-cpu", action="store_true")
+    parser.add_argument("--stages", action="store_true", help="report per-stage device time of the forward kernel")
     parser.add_argument("--profile", action="store_true",
                         help="only warm-up + timed graph replays (for ncu captures); prints nothing else")
     args = parser.parse_args()
@@ -269,6 +270,22 @@ def main():
         end.synchronize()
         kernel_ms.append(start.elapsed_time(end))
     kernel_ms_mean = float(np.mean(kernel_ms))
+
+    # ---- per-stage device time (globaltimer stamps inside the kernel) -------
+    stages = None
+    if args.stages:
+        stamps = torch.zeros((B, 8), dtype=torch.int64, device=device)
+        plan.forward(X, labels=labels, workspace=workspace, status=status, exports={"stage_ns": stamps})
+        torch.cuda.synchronize()
+        st = stamps.cpu().numpy().astype(np.float64)
+        names = ["stage", "prim", "sort", "linkage", "condense", "select_label"]
+        dur = np.diff(st[:, :7], axis=1) / 1e3
+        stages = {name: {"median_us": float(np.median(dur[:, i])), "max_us": float(dur[:, i].max())}
+                  for i, name in enumerate(names)}
+        stages["window_total_us"] = {"median_us": float(np.median(st[:, 6] - st[:, 0]) / 1e3),
+                                     "max_us": float((st[:, 6] - st[:, 0]).max() / 1e3)}
+        n_med = float(np.median(np.diff(offsets)))
+        stages["prim_ns_per_iteration"] = float(np.median(dur[:, 1]) * 1e3 / max(n_med - 1, 1))
 
     # ---- plain per-window launches of the same kernels ----------------------
     plain_plans = {}
@@ -379,6 +396,7 @@ def main():
                      "kernel": "hdb_forward_kernel", "kernel_ms": kernel_ms_mean,
                      "note": "latency-bound (serial Prim/tree chains); algorithmic bytes per launch"},
         "cpu_baseline": cpu,
+        "stages": stages,
         "clocks": clocks.summary(),
         "plan": describe["classes"],
     }

@@ -24,7 +24,7 @@ _lock = threading.Lock()
 _lib = None
 
 EXPORT_FIELDS = ("edges_uv", "edge_w", "order", "link_lr", "link_w", "link_size", "n_clusters", "cl_parent",
-                 "cl_birth", "cl_stability", "cl_selected", "point_parent", "core", "core_nbr")
+                 "cl_birth", "cl_stability", "cl_selected", "point_parent", "core", "core_nbr", "stage_ns")
 
 
 class Exports(ctypes.Structure):

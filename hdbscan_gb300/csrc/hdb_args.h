@@ -21,6 +21,10 @@ struct ForwardArgs {
     int mcs;
     int unit_core;             // ms <= 2
     int x_in_smem;             // stage the window's coordinates in shared memory
+    int n_arenas;              // 1 or 2 hierarchy arenas (2 = Prim/tree overlap)
+    int arena_stride;          // bytes per arena in dynamic shared memory
+    int x_off;                 // byte offset of the staged coordinates
+    int core_off;              // byte offset of the staged core distances
     double eps;
     const void* core;          // [T] Real, or null when unit_core
     const void* dist;          // matrix variant: packed per-window [n, n] Real blocks
@@ -41,6 +45,7 @@ struct ForwardArgs {
     void* cl_stability;        // [T]
     uint8_t* cl_selected;      // [T]
     int32_t* point_parent;     // [T]
+    int64_t* stage_ns;         // [B, 8] globaltimer at stage boundaries (diagnostics)
 };
 
 struct DistanceArgs {

@@ -40,6 +40,8 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 struct WindowClass {
     const hdb::ForwardVariant* fv = nullptr;
     int x_in_smem = 0;
+    int n_arenas = 1;
+    hdb::ForwardLayout layout{};
     std::vector<int> windows;  // descending n
     int nmax = 0;
     size_t smem = 0;
@@ -111,26 +113,28 @@ int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
 
 cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise_dynamic_smem(func, bytes); }
 
-// Autotune table: (threads, vertices per thread) by window size, register
+// Autotune table: (Prim threads, slots per thread) by window size, register
 // dimensions by D.  Windows whose coordinates do not fit the register budget
-// of an instantiated variant use the matrix variant.
+// (64 32-bit registers of coordinates per thread) use the matrix variant.
+void class_shape(int n, int* threads, int* v) {
+    if (n <= 64) { *threads = 32; *v = 2; }
+    else if (n <= 128) { *threads = 64; *v = 2; }
+    else if (n <= 256) { *threads = 128; *v = 2; }
+    else if (n <= 512) { *threads = 256; *v = 2; }
+    else if (n <= 1024) { *threads = 512; *v = 2; }
+    else if (n <= 2048) { *threads = 512; *v = 4; }
+    else { *threads = 512; *v = 8; }
+}
+
 const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int precision, int n, int D,
                                           bool force_matrix) {
     int threads, v;
-    if (n <= 128) { threads = 128; v = 1; }
-    else if (n <= 256) { threads = 256; v = 1; }
-    else if (n <= 512) { threads = 512; v = 1; }
-    else if (n <= 1024) { threads = 512; v = 2; }
-    else if (n <= 2048) { threads = 1024; v = 2; }
-    else { threads = 1024; v = 4; }
+    class_shape(n, &threads, &v);
     int dp = 0;
     if (!force_matrix) {
-        const int options32[] = {8, 16, 32};
-        const int options64[] = {8, 16};
-        const int* options = precision == HDB_F32 ? options32 : options64;
-        const int count = precision == HDB_F32 ? 3 : 2;
-        for (int i = 0; i < count; ++i)
-            if (D <= options[i]) { dp = options[i]; break; }
+        const int words = precision == HDB_F32 ? 1 : 2;  // registers per coordinate
+        for (int option : {8, 16, 32})
+            if (D <= option && v * option * words <= 64) { dp = option; break; }
     }
     const hdb::ForwardVariant* fallback = nullptr;
     for (int i = 0; i < k.n_forward; ++i) {
@@ -140,6 +144,15 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
         if (f.dp == 0) fallback = &f;
     }
     return fallback;
+}
+
+// Dynamic shared memory available to a forward variant next to its static use.
+int smem_budget(const void* func, int optin, size_t* budget) {
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, func);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
+    *budget = (size_t)optin > attr.sharedSizeBytes + 1024 ? (size_t)optin - attr.sharedSizeBytes - 1024 : 0;
+    return HDB_OK;
 }
 
 const hdb::CoreVariant* choose_core(const hdb::PrecisionKernels& k, int precision, int ms, int D, bool matrix) {
@@ -187,22 +200,21 @@ int build_plan(hdb_plan* p) {
         const int n = size_of(w);
         const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, force_matrix);
         if (!fv) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(n) + " points");
-        const bool static_ok = true;
-        (void)static_ok;
-        int xs = fv->dp > 0 ? 1 : 0;
-        size_t smem = k.forward_smem(n, fv->dp, xs, unit);
-        const size_t budget = (size_t)optin - 2048;  // leave room for static shared memory
-        if (smem > budget && xs) { xs = 0; smem = k.forward_smem(n, fv->dp, false, unit); }
-        if (smem > budget)
+        size_t budget = 0;
+        int rc = smem_budget(fv->func, optin, &budget);
+        if (rc) return rc;
+        hdb::ForwardLayout layout{};
+        if (!k.forward_layout(n, fv->dp, unit, budget, &layout))
             return fail(HDB_E_INVALID, "window of " + std::to_string(n) + " points exceeds shared memory");
         WindowClass* cls = nullptr;
         for (auto& c : p->classes)
-            if (c.fv == fv && c.x_in_smem == xs) { cls = &c; break; }
+            if (c.fv == fv && c.x_in_smem == layout.x_in_smem && c.n_arenas == layout.n_arenas) { cls = &c; break; }
         if (!cls) {
             p->classes.emplace_back();
             cls = &p->classes.back();
             cls->fv = fv;
-            cls->x_in_smem = xs;
+            cls->x_in_smem = layout.x_in_smem;
+            cls->n_arenas = layout.n_arenas;
         }
         cls->windows.push_back(w);
         cls->nmax = std::max(cls->nmax, n);
@@ -262,10 +274,16 @@ int build_plan(hdb_plan* p) {
 
     // ---- grids --------------------------------------------------------------
     for (auto& c : p->classes) {
-        c.smem = k.forward_smem(c.nmax, c.fv->dp, c.x_in_smem, unit);
+        size_t budget = 0;
+        int rc = smem_budget(c.fv->func, optin, &budget);
+        if (rc) return rc;
+        if (!k.forward_layout(c.nmax, c.fv->dp, unit, budget, &c.layout) || c.layout.n_arenas != c.n_arenas ||
+            c.layout.x_in_smem != c.x_in_smem)
+            return fail(HDB_E_INVALID, "inconsistent shared-memory layout for a window class");
+        c.smem = c.layout.bytes;
         HDB_CUDA(raise_smem_limit(c.fv->func, c.smem));
         int per_sm = 0;
-        HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads, c.smem));
+        HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads + 32, c.smem));
         if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
         c.grid = (int)std::min<size_t>(c.windows.size(), (size_t)per_sm * p->sms);
     }
@@ -409,6 +427,10 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.mcs = p->mcs;
         a.unit_core = unit ? 1 : 0;
         a.x_in_smem = c.x_in_smem;
+        a.n_arenas = c.layout.n_arenas;
+        a.arena_stride = (int)c.layout.arena_stride;
+        a.x_off = (int)c.layout.x_off;
+        a.core_off = (int)c.layout.core_off;
         a.eps = p->eps;
         a.core = unit ? nullptr : core;
         a.dist = dist;
@@ -429,6 +451,7 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.cl_stability = ex->cl_stability;
         a.cl_selected = ex->cl_selected;
         a.point_parent = ex->point_parent;
+        a.stage_ns = ex->stage_ns;
         if (a.cl_parent && (!a.cl_birth || !a.cl_stability || !a.cl_selected || !a.point_parent || !a.n_clusters))
             return fail(HDB_E_INVALID, "cl_parent needs cl_birth, cl_stability, cl_selected, point_parent, n_clusters");
         cudaStream_t s = (fork && i > 0) ? p->aux[i - 1] : stream;
@@ -571,7 +594,8 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
         s += (i ? "," : "") + std::string("{\"threads\":") + std::to_string(c.fv->threads) +
              ",\"vertices_per_thread\":" + std::to_string(c.fv->v) + ",\"register_dims\":" +
              std::to_string(c.fv->dp) + ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
-             "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"windows\":" +
+             "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
+             ",\"windows\":" +
              std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
              std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";
     }

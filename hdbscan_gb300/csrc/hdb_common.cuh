@@ -23,6 +23,7 @@ template <> struct RealTraits<float> {
     __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
     __device__ __forceinline__ static float sub(float a, float b) { return __fsub_rn(a, b); }
     __device__ __forceinline__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+    __device__ __forceinline__ static float mul_ru(float a, float b) { return __fmul_ru(a, b); }
     __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
     __device__ __forceinline__ static float sqrt_rn(float a) { return __fsqrt_rn(a); }
     __device__ __forceinline__ static float recip(float a) { return __fdiv_rn(1.0f, a); }
@@ -39,6 +40,7 @@ template <> struct RealTraits<double> {
     __device__ __forceinline__ static double inf() { return __longlong_as_double(0x7ff0000000000000ll); }
     __device__ __forceinline__ static double sub(double a, double b) { return __dsub_rn(a, b); }
     __device__ __forceinline__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+    __device__ __forceinline__ static double mul_ru(double a, double b) { return __dmul_ru(a, b); }
     __device__ __forceinline__ static double add(double a, double b) { return __dadd_rn(a, b); }
     __device__ __forceinline__ static double sqrt_rn(double a) { return __dsqrt_rn(a); }
     __device__ __forceinline__ static double recip(double a) { return __ddiv_rn(1.0, a); }

@@ -1,279 +1,444 @@
-// Fused per-window forward kernel: Prim MST over the mutual-reachability
-// graph (distances recomputed on chip, never written to HBM) followed by the
-// hierarchy stages of hdb_tree.cuh, persistent over a size-sorted work queue.
+// Fused per-window forward kernel, warp-specialized and persistent.
 //
 // Reference path replaced: hdbscan_gpu/_cuda.py:110-127 (dense distance
 // buffer + cluster kernel) and hdbscan_gpu/_kernels.py:164-760.
 //
-// Prim (reference _kernels.py:164-320, register variant :194-209):
-//  * each thread owns V vertices j = tid + v*THREADS with their coordinates
-//    (padded to DP, zero padding is exact) in registers, best weight, source
-//    and an in-tree bit;
-//  * per iteration the current vertex's coordinates come from the window
-//    staged in shared memory (or from global memory for large windows);
-//  * DP == 0 selects the matrix variant instead: weights come from row
-//    `current` of a materialized distance matrix (hdb_distance.cuh), read
-//    coalesced, exactly as the reference reads distances[current*n + j];
-//  * strict '<' update keeps the older source on equal weights;
-//  * argmin by (weight, vertex index) with redux.sync in every warp, warp
-//    winners double-buffered in shared memory, ONE __syncthreads per
-//    iteration, and every warp re-reduces the warp winners so the next
-//    vertex is known without a second barrier;
-//  * the owner of the winning vertex writes the edge (source, vertex, weight).
+// One CTA = PT "Prim" threads + one "tree" warp, looping over a size-sorted
+// window queue (atomic ticket, bounded by the queue length):
+//  * the Prim warps build window k's minimum spanning tree of the
+//    mutual-reachability graph (reference _kernels.py:164-320) into arena k%2;
+//  * the tree warp turns window k-1's edges into labels (hdb_tree.cuh) in the
+//    other arena at the same time.
+// Hand-off uses named barriers only (bar.arrive / bar.sync with fixed thread
+// counts): FULL[b] (Prim arrives, tree waits) and EMPTY[b] (tree arrives, Prim
+// waits before reusing arena b).  With one arena (large windows) the two
+// roles simply alternate.
+//
+// Prim details:
+//  * slot s lives in thread s / SV (vertex id vid); the thread keeps the
+//    vertex's coordinates (zero-padded to DP, exact) in registers, its best
+//    weight, source and an in-tree bit;
+//  * the current vertex's coordinates come from the window staged in shared
+//    memory (or from global memory for large windows); DP == 0 selects the
+//    matrix variant, which reads row `current` of a materialized distance
+//    block instead (hdb_distance.cuh);
+//  * strict '<' update keeps the older source on equal weights; argmin by
+//    (weight, vertex id) with redux.sync, one barrier per iteration, every
+//    active warp re-reduces the warp winners so the next vertex is known
+//    without a second barrier;
+//  * a candidate skips the correctly rounded sqrt when acc >= RU(best^2):
+//    then sqrt_rn(acc) >= best (sqrt_rn is monotone, best representable), so
+//    no strict improvement is possible;
+//  * whenever a warp's worth of slots has joined the tree, the vertices still
+//    outside are re-packed into the lowest slots and the warps left without
+//    slots stop taking part in the iteration barrier.
 #pragma once
 #include "hdb_common.cuh"
 #include "hdb_tree.cuh"
 
 namespace hdb {
 
+constexpr int kBarStart = 1;  // Prim threads: window start / staging / post-Prim
+constexpr int kBarIter = 2;   // active Prim warps: per-iteration barrier
+constexpr int kBarFull = 3;   // 3, 4: Prim -> tree hand-off of arena 0 / 1
+constexpr int kBarEmpty = 5;  // 5, 6: tree -> Prim release of arena 0 / 1
 
-template <typename Real, int DP>
-__host__ __device__ constexpr int stage_stride() { return DP > 0 ? DP : 1; }
-
-// Bytes of dynamic shared memory for a window of n points.
-template <typename Real, int DP>
-__host__ __device__ inline size_t forward_smem_bytes(int n, bool x_in_smem, bool unit_core) {
-    size_t bytes = Arena<Real>::bytes(n);
-    bytes = (bytes + 15) & ~size_t(15);
-    if (x_in_smem && DP > 0) bytes += (size_t)n * DP * sizeof(Real);
-    if (!unit_core) bytes += (size_t)Arena<Real>::round_cap(n) * sizeof(Real);
-    return bytes;
+__device__ __forceinline__ void bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-template <typename Real, int THREADS, int V, int DP>
-__global__ void __launch_bounds__(THREADS) hdb_forward_kernel(const ForwardArgs args) {
+__device__ __forceinline__ int64_t global_ns() {
+    int64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Exclusive scan of one int per thread over the first `warps` warps (all of
+// them must call); `total` receives the sum.  Uses barrier kBarIter.
+__device__ __forceinline__ int active_exclusive_scan(int value, int warps, int* s_scan, int& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = value;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_scan[warp] = x;
+    bar_sync(kBarIter, warps * 32);
+    int t = lane < warps ? s_scan[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+    }
+    total = __shfl_sync(0xffffffffu, t, 31);
+    const int before = __shfl_sync(0xffffffffu, t, warp > 0 ? warp - 1 : 0);
+    return (warp > 0 ? before : 0) + x - value;
+}
+
+// Coordinates of vertex j (padded to DPS with zeros) into registers.
+template <typename Real, int DP, int DPS, int VEC>
+__device__ __forceinline__ void load_coords(Real (&xr)[DPS], int j, bool xs, const Real* s_x, const Real* Xw, int D) {
+    if (DP == 0) return;
+    if (j < 0) {
+#pragma unroll
+        for (int k = 0; k < DPS; ++k) xr[k] = Real(0);
+        return;
+    }
+    if (xs) {
+#pragma unroll
+        for (int k0 = 0; k0 < DPS; k0 += VEC) {
+            if constexpr (sizeof(Real) == 4) {
+                const float4 q = *reinterpret_cast<const float4*>(s_x + j * DPS + k0);
+                xr[k0] = q.x; xr[(k0 + 1) % DPS] = q.y; xr[(k0 + 2) % DPS] = q.z; xr[(k0 + 3) % DPS] = q.w;
+            } else {
+                const double2 q = *reinterpret_cast<const double2*>(s_x + j * DPS + k0);
+                xr[k0] = q.x; xr[(k0 + 1) % DPS] = q.y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < DPS; ++k) xr[k] = k < D ? Xw[(int64_t)j * D + k] : Real(0);
+    }
+}
+
+struct WindowMeta {
+    int w;      // window index, -1 = queue exhausted
+    int n;
+    int skip;   // labels already written (invalid input / overflow)
+};
+
+// Dynamic shared memory: n_arenas arenas of arena_stride bytes, then the
+// staged window (x_off) and its core distances (core_off); see the plan layer.
+template <typename Real, int PT, int SV, int DP>
+__global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs args) {
     using T = RealTraits<Real>;
     using Key = typename T::Bits;
-    constexpr int NW = THREADS / 32;
+    constexpr int PW = PT / 32;
     constexpr int VEC = 16 / (int)sizeof(Real);
-    static_assert(DP % VEC == 0, "DP must be a multiple of one 16-byte vector");
+    constexpr int DPS = DP > 0 ? DP : VEC;
+    static_assert(DPS % VEC == 0, "DP must be a multiple of one 16-byte vector");
+    static_assert(PT % 32 == 0 && PT + 32 <= 1024, "Prim threads plus the tree warp must fit one CTA");
+    static_assert(SV <= 16, "in-tree bits are kept in one 16-bit mask");
     constexpr Key SENTINEL = (Key)~(Key)0;
-    constexpr int DPS = DP > 0 ? DP : 1;  // stride of the staged window
 
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ Key s_key[2][NW];
-    __shared__ uint32_t s_idx[2][NW];
+    __shared__ Key s_key[2][PW];
+    __shared__ uint32_t s_idx[2][PW];
+    __shared__ int s_scan[32];
     __shared__ int s_item;
-    __shared__ int s_counter;
-    __shared__ int s_next_label;
+    __shared__ int s_flags[2];  // by window parity: a reset never races a late read
+    __shared__ WindowMeta s_meta[2];
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
     const Real* __restrict__ X = static_cast<const Real*>(args.X);
-    const Real* __restrict__ core_g = static_cast<const Real*>(args.core);
     const int D = args.D;
-    const Real epsilon = (Real)args.eps;  // the reference casts options to Real (_cuda.py:105)
+    const int nb = args.n_arenas;
 
-    for (int guard = 0; guard < (1 << 30); ++guard) {
-        if (tid == 0) s_item = atomicAdd(args.ticket, 1);
-        __syncthreads();
+    if (warp == PW) {
+        // =================== tree warp (consumer) ============================
+        const Real epsilon = (Real)args.eps;  // the reference casts options to Real (_cuda.py:105)
+        for (int k = 0; k < (1 << 30); ++k) {
+            const int b = nb == 2 ? (k & 1) : 0;
+            bar_sync(kBarFull + b, PT + 32);
+            const WindowMeta meta = s_meta[b];
+            if (meta.w < 0) return;
+            if (!meta.skip) {
+                const int w = meta.w, n = meta.n, m = n - 1;
+                const int64_t base = args.offsets[w];
+                const int64_t ebase = base - w;
+                Arena<Real> a = Arena<Real>::carve(smem + (size_t)b * args.arena_stride, n);
+                if (args.edges_uv) {
+                    for (int i = lane; i < m; i += 32) {
+                        args.edges_uv[2 * (ebase + i)] = a.s0[i];
+                        args.edges_uv[2 * (ebase + i) + 1] = a.s1[i];
+                        static_cast<Real*>(args.edge_w)[ebase + i] = a.r0[i];
+                    }
+                }
+                sort_edges_warp<Real>(a, m);
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 3] = global_ns();
+                if (args.order)
+                    for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
+                __syncwarp();
+                for (int i = lane; i < m; i += 32) {
+                    const int e = a.s2[i];
+                    const int16_t u = a.s0[e], v = a.s1[e];
+                    a.s2[i] = u;
+                    a.s3[i] = v;
+                }
+                __syncwarp();
+                linkage_warp<Real>(a, n);
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
+                if (args.link_lr) {
+                    for (int i = lane; i < m; i += 32) {
+                        args.link_lr[2 * (ebase + i)] = a.s4[i];
+                        args.link_lr[2 * (ebase + i) + 1] = a.s5[i];
+                        args.link_size[ebase + i] = a.s6[i];
+                        static_cast<Real*>(args.link_w)[ebase + i] = a.r0[i];
+                    }
+                }
+                __syncwarp();
+                const int next_label = condense_warp<Real>(a, n, args.mcs);
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 5] = global_ns();
+                if (args.cl_parent) {
+                    for (int c = lane; c < next_label - n; c += 32) {
+                        args.cl_parent[base + c] = a.s2[c];
+                        static_cast<Real*>(args.cl_birth)[base + c] = a.r1[c];
+                    }
+                }
+                __syncwarp();
+                select_and_label_warp<Real>(a, n, next_label, epsilon, args.labels + base);
+                if (args.cl_parent) {
+                    for (int c = lane; c < next_label - n; c += 32) {
+                        static_cast<Real*>(args.cl_stability)[base + c] = a.r2[c];
+                        args.cl_selected[base + c] = a.sel[c];
+                    }
+                    for (int i = lane; i < n; i += 32) args.point_parent[base + i] = a.s9[i];
+                    if (lane == 0) args.n_clusters[w] = next_label - n;
+                }
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
+            }
+            __syncwarp();
+            __threadfence_block();
+            bar_arrive(kBarEmpty + b, PT + 32);
+        }
+        return;
+    }
+
+    // ====================== Prim warps (producer) ============================
+    const Real* __restrict__ core_g = static_cast<const Real*>(args.core);
+    const bool xs = DP > 0 && args.x_in_smem;
+    Real* s_x = reinterpret_cast<Real*>(smem + args.x_off);
+    Real* s_core = reinterpret_cast<Real*>(smem + args.core_off);
+
+    for (int k = 0; k < (1 << 30); ++k) {
+        const int b = nb == 2 ? (k & 1) : 0;
+        const int par = k & 1;
+        if (tid == 0) { s_item = atomicAdd(args.ticket, 1); s_flags[par] = 0; }
+        bar_sync(kBarStart, PT);
         const int item = s_item;
-        if (item >= args.queue_len) return;
+        if (item >= args.queue_len) {
+            if (k >= nb) bar_sync(kBarEmpty + b, PT + 32);
+            if (tid == 0) s_meta[b].w = -1;
+            __threadfence_block();
+            bar_arrive(kBarFull + b, PT + 32);
+            // Take the tree warp's release of the previous window so no
+            // arrival is left pending when the CTA exits.
+            if (nb == 2 && k >= 1) bar_sync(kBarEmpty + (b ^ 1), PT + 32);
+            return;
+        }
         const int w = args.queue[item];
         const int64_t base = args.offsets[w];
         const int n = (int)(args.offsets[w + 1] - base);
         const Real* __restrict__ Xw = X + base * D;
         const Real* __restrict__ Dw = DP > 0 ? nullptr : static_cast<const Real*>(args.dist) + args.dist_offsets[w];
+        if (args.stage_ns && tid == 0) args.stage_ns[8 * w + 0] = global_ns();
 
-        // ---- shared-memory carve-up ------------------------------------
-        Arena<Real> arena = Arena<Real>::carve(smem, n);
-        size_t off = (Arena<Real>::bytes(n) + 15) & ~size_t(15);
-        Real* s_x = nullptr;
-        const bool xs = DP > 0 && args.x_in_smem;
-        if (xs) { s_x = reinterpret_cast<Real*>(smem + off); off += (size_t)n * DP * sizeof(Real); }
-        Real* s_core = nullptr;
-        if (!args.unit_core) s_core = reinterpret_cast<Real*>(smem + off);
-
-        // ---- stage coordinates / cores, validate input ------------------
+        // ---- stage coordinates / cores, validate input -----------------------
         int bad = 0;
         if (xs) {
-            for (int t = tid; t < n * DPS; t += THREADS) {
-                const int j = t / DPS, k = t - j * DPS;
+            for (int t = tid; t < n * DPS; t += PT) {
+                const int j = t / DPS, kk = t - j * DPS;
                 Real v = Real(0);
-                if (k < D) { v = Xw[(int64_t)j * D + k]; bad |= !isfinite(v); }
+                if (kk < D) { v = Xw[(int64_t)j * D + kk]; bad |= !isfinite(v); }
                 s_x[t] = v;
             }
         } else {
-            for (int t = tid; t < n * D; t += THREADS) bad |= !isfinite(Xw[t]);
+            for (int t = tid; t < n * D; t += PT) bad |= !isfinite(Xw[t]);
         }
         if (!args.unit_core)
-            for (int j = tid; j < n; j += THREADS) s_core[j] = core_g[base + j];
-        if (__syncthreads_or(bad)) {
-            if (tid == 0) atomic_status(args.status, kNonFinite);
-            for (int j = tid; j < n; j += THREADS) args.labels[base + j] = -1;
-            continue;
-        }
+            for (int j = tid; j < n; j += PT) s_core[j] = core_g[base + j];
+        if (bad) atomicOr(&s_flags[par], 1);
+        bar_sync(kBarStart, PT);
+        const bool invalid = s_flags[par] & 1;
 
-        Real xr[V][DP > 0 ? DP : 1];
-        Real best[V];
-        Real core_r[V];
-        int src[V];
-        uint32_t in_tree = 0;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const int j = tid + v * THREADS;
-            best[v] = T::inf();
-            src[v] = 1;  // reference initial source (_kernels.py:167)
-            core_r[v] = Real(0);
-            if (DP > 0) {
-#pragma unroll
-                for (int k = 0; k < (DP > 0 ? DP : 1); ++k) {
-                    Real value = Real(0);
-                    if (j < n) value = xs ? s_x[j * DPS + k] : (k < D ? Xw[(int64_t)j * D + k] : Real(0));
-                    xr[v][k] = value;
-                }
-            }
-            if (!args.unit_core && j < n) core_r[v] = s_core[j];
-        }
-        if (tid == 0) in_tree = 1u;  // vertex 0 starts the tree (_kernels.py:210-213)
+        if (k >= nb) bar_sync(kBarEmpty + b, PT + 32);  // arena b released by the tree warp
+        Arena<Real> arena = Arena<Real>::carve(smem + (size_t)b * args.arena_stride, n);
 
-        // ---- Prim -------------------------------------------------------
-        int cur = 0;
         int overflow = 0;
-        for (int it = 0; it < n - 1; ++it) {
-            const Real core_cur = args.unit_core ? Real(0) : s_core[cur];
-            Real acc[V];
+        if (!invalid) {
+            Real xr[SV][DPS];
+            Real best[SV];
+            Real thr[SV];  // RU(best^2)
+            Real core_r[SV];
+            int src[SV];
+            int vid[SV];
+            uint32_t in_tree = 0;
 #pragma unroll
-            for (int v = 0; v < V; ++v) acc[v] = Real(0);
-            if (DP > 0) {
+            for (int v = 0; v < SV; ++v) {
+                const int j = tid * SV + v;
+                vid[v] = j < n ? j : -1;
+                best[v] = T::inf();
+                thr[v] = T::inf();
+                src[v] = 1;  // reference initial source (_kernels.py:167)
+                core_r[v] = Real(0);
+                load_coords<Real, DP, DPS, VEC>(xr[v], vid[v], xs, s_x, Xw, D);
+                if (!args.unit_core && j < n) core_r[v] = s_core[j];
+            }
+            if (tid == 0) in_tree = 1u;  // vertex 0 starts the tree (_kernels.py:210-213)
+            if (args.stage_ns && tid == 0) args.stage_ns[8 * w + 1] = global_ns();
+
+            int cur = 0;
+            Real acc_max = Real(0);
+            int live = n;
+            int aw = (n + 32 * SV - 1) / (32 * SV);  // active warps
+            if (aw > PW) aw = PW;
+            if (warp < aw) {
+                for (int it = 0; it < n - 1; ++it) {
+                    const int remaining = n - 1 - it;  // vertices still outside the tree
+                    if (live - remaining >= 32 * SV) {
+                        // ---- compaction over the active warps --------------
+                        int count = 0;
 #pragma unroll
-                for (int k0 = 0; k0 < (DP > 0 ? DP : VEC); k0 += VEC) {
-                    Real c[VEC];
-                    if (xs) {
-                        if constexpr (sizeof(Real) == 4) {
-                            const float4 q = *reinterpret_cast<const float4*>(s_x + cur * DPS + k0);
-                            c[0] = q.x; c[1] = q.y; c[2 % VEC] = q.z; c[3 % VEC] = q.w;
-                        } else {
-                            const double2 q = *reinterpret_cast<const double2*>(s_x + cur * DPS + k0);
-                            c[0] = q.x; c[1 % VEC] = q.y;
+                        for (int v = 0; v < SV; ++v)
+                            count += (tid * SV + v < live && !((in_tree >> v) & 1u)) ? 1 : 0;
+                        int total = 0;
+                        int pos = active_exclusive_scan(count, aw, s_scan, total);
+                        int16_t* stage_j = arena.s2;
+                        int16_t* stage_src = arena.s3;
+                        Real* stage_best = arena.r1;
+#pragma unroll
+                        for (int v = 0; v < SV; ++v) {
+                            if (tid * SV + v < live && !((in_tree >> v) & 1u)) {
+                                stage_j[pos] = (int16_t)vid[v];
+                                stage_src[pos] = (int16_t)src[v];
+                                stage_best[pos] = best[v];
+                                ++pos;
+                            }
+                        }
+                        bar_sync(kBarIter, aw * 32);
+                        live = total;
+                        in_tree = 0;
+#pragma unroll
+                        for (int v = 0; v < SV; ++v) {
+                            const int slot = tid * SV + v;
+                            if (slot < live) {
+                                vid[v] = stage_j[slot];
+                                src[v] = stage_src[slot];
+                                best[v] = stage_best[slot];
+                                thr[v] = T::mul_ru(best[v], best[v]);
+                                if (!args.unit_core) core_r[v] = s_core[vid[v]];
+                                load_coords<Real, DP, DPS, VEC>(xr[v], vid[v], xs, s_x, Xw, D);
+                            } else {
+                                vid[v] = -1;
+                            }
+                        }
+                        bar_sync(kBarIter, aw * 32);  // staging slots may be rewritten afterwards
+                        const int naw = (live + 32 * SV - 1) / (32 * SV);
+                        aw = naw < 1 ? 1 : naw;
+                        if (warp >= aw) break;  // this warp has no slots left (warp-uniform)
+                    }
+                    const Real core_cur = args.unit_core ? Real(0) : s_core[cur];
+                    Real acc[SV];
+#pragma unroll
+                    for (int v = 0; v < SV; ++v) acc[v] = Real(0);
+                    if (DP > 0) {
+#pragma unroll
+                        for (int k0 = 0; k0 < DPS; k0 += VEC) {
+                            Real c[VEC];
+                            if (xs) {
+                                if constexpr (sizeof(Real) == 4) {
+                                    const float4 q = *reinterpret_cast<const float4*>(s_x + cur * DPS + k0);
+                                    c[0] = q.x; c[1] = q.y; c[2 % VEC] = q.z; c[3 % VEC] = q.w;
+                                } else {
+                                    const double2 q = *reinterpret_cast<const double2*>(s_x + cur * DPS + k0);
+                                    c[0] = q.x; c[1 % VEC] = q.y;
+                                }
+                            } else {
+#pragma unroll
+                                for (int kk = 0; kk < VEC; ++kk)
+                                    c[kk] = (k0 + kk < D) ? Xw[(int64_t)cur * D + k0 + kk] : Real(0);
+                            }
+#pragma unroll
+                            for (int v = 0; v < SV; ++v) {
+#pragma unroll
+                                for (int kk = 0; kk < VEC; ++kk) {
+                                    const Real delta = T::sub(c[kk], xr[v][(k0 + kk) % DPS]);
+                                    acc[v] = T::add(acc[v], T::mul(delta, delta));
+                                }
+                            }
                         }
                     } else {
+                        // Matrix variant: row `cur` of the window's distance block.
+                        const Real* __restrict__ row = Dw + (int64_t)cur * (int64_t)((n + 3) & ~3);
 #pragma unroll
-                        for (int kk = 0; kk < VEC; ++kk)
-                            c[kk] = (k0 + kk < D) ? Xw[(int64_t)cur * D + k0 + kk] : Real(0);
+                        for (int v = 0; v < SV; ++v)
+                            if (tid * SV + v < live && !((in_tree >> v) & 1u)) acc[v] = __ldcg(row + vid[v]);
                     }
+                    Key lkey = SENTINEL;
+                    uint32_t lidx = 0xffffffffu;
 #pragma unroll
-                    for (int v = 0; v < V; ++v) {
-#pragma unroll
-                        for (int kk = 0; kk < VEC; ++kk) {
-                            const Real delta = T::sub(c[kk], xr[v][(k0 + kk) % (DP > 0 ? DP : 1)]);
-                            acc[v] = T::add(acc[v], T::mul(delta, delta));
+                    for (int v = 0; v < SV; ++v) {
+                        if (tid * SV + v < live && !((in_tree >> v) & 1u)) {
+                            if (DP > 0) {
+                                acc_max = T::maxr(acc_max, acc[v]);
+                                const Real cm = args.unit_core ? Real(0) : T::maxr(core_cur, core_r[v]);
+                                if (cm < best[v] && acc[v] < thr[v]) {
+                                    const Real d = T::sqrt_rn(acc[v]);
+                                    const Real wgt = T::maxr(cm, d);
+                                    if (wgt < best[v]) {
+                                        best[v] = wgt;
+                                        src[v] = cur;
+                                        thr[v] = T::mul_ru(wgt, wgt);
+                                    }
+                                }
+                            } else {
+                                const Real d = acc[v];
+                                overflow |= !(d <= T::kMax);
+                                const Real wgt = args.unit_core ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
+                                if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
+                            }
+                            const Key key = T::key(best[v]);
+                            const uint32_t j = (uint32_t)vid[v];
+                            if (key < lkey || (key == lkey && j < lidx)) { lkey = key; lidx = j; }
                         }
                     }
-                }
-            } else {
-                // Matrix variant: row `cur` of the window's distance block.
-                const Real* __restrict__ row = Dw + (int64_t)cur * (int64_t)((n + 3) & ~3);  // padded stride
+                    warp_argmin(lkey, lidx);
+                    const int buf = it & 1;
+                    if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
+                    bar_sync(kBarIter, aw * 32);
+                    Key gk = lane < aw ? s_key[buf][lane] : SENTINEL;
+                    uint32_t gi = lane < aw ? s_idx[buf][lane] : 0xffffffffu;
+                    warp_argmin(gk, gi);
+                    const int next = (int)gi;
+                    // Owner of the winner records the edge and joins the tree.
 #pragma unroll
-                for (int v = 0; v < V; ++v) {
-                    const int j = tid + v * THREADS;
-                    if (j < n && !((in_tree >> v) & 1u)) acc[v] = __ldcg(row + j);
-                }
-            }
-            Key lkey = SENTINEL;
-            uint32_t lidx = 0xffffffffu;
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int j = tid + v * THREADS;
-                if (j < n && !((in_tree >> v) & 1u)) {
-                    const Real d = DP > 0 ? T::sqrt_rn(acc[v]) : acc[v];
-                    overflow |= !(d <= T::kMax);
-                    const Real wgt = args.unit_core ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
-                    if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
-                    const Key k = T::key(best[v]);
-                    if (k < lkey) { lkey = k; lidx = (uint32_t)j; }
-                }
-            }
-            warp_argmin(lkey, lidx);
-            const int buf = it & 1;
-            if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
-            __syncthreads();
-            Key gk = lane < NW ? s_key[buf][lane] : SENTINEL;
-            uint32_t gi = lane < NW ? s_idx[buf][lane] : 0xffffffffu;
-            warp_argmin(gk, gi);
-            const int next = (int)gi;
-            // Owner of the winner records the edge and joins the tree.
-            if ((next % THREADS) == tid) {
-                const int v = next / THREADS;
-#pragma unroll
-                for (int vv = 0; vv < V; ++vv) {
-                    if (vv == v) {
-                        arena.s0[it] = (int16_t)src[vv];
-                        arena.s1[it] = (int16_t)next;
-                        arena.r0[it] = best[vv];
-                        in_tree |= 1u << vv;
+                    for (int v = 0; v < SV; ++v) {
+                        if (vid[v] == next && tid * SV + v < live) {
+                            arena.s0[it] = (int16_t)src[v];
+                            arena.s1[it] = (int16_t)next;
+                            arena.r0[it] = best[v];
+                            in_tree |= 1u << v;
+                        }
                     }
+                    if (next < 0 || next >= n) {  // unreachable: a non-tree vertex always remains
+                        overflow |= 2;
+                        break;
+                    }
+                    cur = next;
                 }
             }
-            if (next < 0 || next >= n) {  // unreachable: one non-tree vertex always remains
-                overflow |= 2;
-                break;
-            }
-            cur = next;
+            if (DP > 0) overflow |= !(acc_max <= T::kMax);
         }
-        if (__syncthreads_or(overflow)) {
-            if (tid == 0) atomic_status(args.status, (overflow & 2) ? kInternal : kOverflow);
-            for (int j = tid; j < n; j += THREADS) args.labels[base + j] = -1;
-            continue;
+        if (overflow) atomicOr(&s_flags[par], overflow << 1);
+        bar_sync(kBarStart, PT);
+        const int flags = s_flags[par];
+        if (args.stage_ns && tid == 0) args.stage_ns[8 * w + 2] = global_ns();
+        int skip = 0;
+        if (flags) {
+            const int code = (flags & 1) ? kNonFinite : ((flags & 4) ? kInternal : kOverflow);
+            if (tid == 0) atomic_status(args.status, code);
+            for (int j = tid; j < n; j += PT) args.labels[base + j] = -1;
+            skip = 1;
         }
-
-        const int m = n - 1;
-        const int64_t ebase = base - w;
-        if (args.edges_uv) {
-            for (int i = tid; i < m; i += THREADS) {
-                args.edges_uv[2 * (ebase + i)] = arena.s0[i];
-                args.edges_uv[2 * (ebase + i) + 1] = arena.s1[i];
-                static_cast<Real*>(args.edge_w)[ebase + i] = arena.r0[i];
-            }
-        }
-
-        // ---- hierarchy ---------------------------------------------------
-        sort_edges<Real>(arena, m, &s_counter);
-        if (args.order)
-            for (int i = tid; i < m; i += THREADS) args.order[ebase + i] = arena.s2[i];
-        for (int i = tid; i < m; i += THREADS) {
-            const int e = arena.s2[i];
-            const int16_t u = arena.s0[e], v = arena.s1[e];
-            arena.s2[i] = u;
-            arena.s8[i] = v;
-        }
-        for (int i = tid; i < n; i += THREADS) { arena.s6[i] = (int16_t)i; arena.s7[i] = (int16_t)i; }
-        __syncthreads();
-        if (tid == 0) linkage_serial<Real>(arena, n);
-        __syncthreads();
-        if (args.link_lr) {
-            for (int i = tid; i < m; i += THREADS) {
-                args.link_lr[2 * (ebase + i)] = arena.s3[i];
-                args.link_lr[2 * (ebase + i) + 1] = arena.s4[i];
-                args.link_size[ebase + i] = arena.s5[i];
-                static_cast<Real*>(args.link_w)[ebase + i] = arena.r0[i];
-            }
-        }
-        __syncthreads();
-        if (tid == 0) s_next_label = condense_serial<Real>(arena, n, args.mcs);
-        __syncthreads();
-        const int next_label = s_next_label;
-        if (args.cl_parent) {
-            // Condensed state before selection overwrites the arrays it shares.
-            for (int c = tid; c < next_label - n; c += THREADS) {
-                args.cl_parent[base + c] = c == 0 ? -1 : arena.s8[c];
-                static_cast<Real*>(args.cl_birth)[base + c] = arena.r1[c];
-            }
-        }
-        __syncthreads();
-        if (tid == 0) select_and_label<Real>(arena, n, next_label, epsilon, nullptr);
-        __syncthreads();
-        for (int i = tid; i < n; i += THREADS) args.labels[base + i] = arena.s6[arena.s9[i] - n];
-        if (args.cl_parent) {
-            for (int c = tid; c < next_label - n; c += THREADS) {
-                static_cast<Real*>(args.cl_stability)[base + c] = arena.r2[c];
-                args.cl_selected[base + c] = arena.sel[c];
-            }
-            for (int i = tid; i < n; i += THREADS) args.point_parent[base + i] = arena.s9[i];
-            if (tid == 0) args.n_clusters[w] = next_label - n;
-        }
-        __syncthreads();
+        if (tid == 0) { s_meta[b].w = w; s_meta[b].n = n; s_meta[b].skip = skip; }
+        __threadfence_block();
+        bar_arrive(kBarFull + b, PT + 32);
     }
 }
 

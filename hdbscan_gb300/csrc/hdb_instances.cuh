@@ -10,7 +10,7 @@ namespace hdb {
 
 template <typename Real, int THREADS, int V, int DP>
 void launch_forward(const ForwardArgs& a, int grid, size_t smem, cudaStream_t s) {
-    hdb_forward_kernel<Real, THREADS, V, DP><<<grid, THREADS, smem, s>>>(a);
+    hdb_forward_kernel<Real, THREADS, V, DP><<<grid, THREADS + 32, smem, s>>>(a);
 }
 
 template <typename Real, int THREADS, int V, int DP>
@@ -54,13 +54,29 @@ void launch_backward(const BackwardArgs& a, int grid, cudaStream_t s) {
     hdb_backward_kernel<Real><<<grid, 256, 0, s>>>(a);
 }
 
+// Two arenas (Prim/tree overlap) when they fit next to the staged window,
+// else one arena with the staged window, else one arena alone.
 template <typename Real>
-size_t forward_smem_dispatch(int n, int dp, bool x_in_smem, bool unit_core) {
-    size_t bytes = Arena<Real>::bytes(n);
-    bytes = (bytes + 15) & ~size_t(15);
-    if (x_in_smem && dp > 0) bytes += (size_t)n * dp * sizeof(Real);
-    if (!unit_core) bytes += (size_t)Arena<Real>::round_cap(n) * sizeof(Real);
-    return bytes;
+bool forward_layout(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out) {
+    const size_t arena = (Arena<Real>::bytes(n) + 127) & ~size_t(127);
+    const size_t x = dp > 0 ? (((size_t)n * dp * sizeof(Real) + 127) & ~size_t(127)) : 0;
+    const size_t core = unit_core ? 0 : (((size_t)Arena<Real>::round_cap(n) * sizeof(Real) + 127) & ~size_t(127));
+    const int nbs[3] = {2, 1, 1};
+    const int xss[3] = {1, 1, 0};
+    for (int c = 0; c < 3; ++c) {
+        const int xs = dp > 0 ? xss[c] : 0;
+        const size_t bytes = nbs[c] * arena + (xs ? x : 0) + core;
+        if (bytes <= budget) {
+            out->n_arenas = nbs[c];
+            out->x_in_smem = xs;
+            out->arena_stride = arena;
+            out->x_off = nbs[c] * arena;
+            out->core_off = out->x_off + (xs ? x : 0);
+            out->bytes = bytes;
+            return true;
+        }
+    }
+    return false;
 }
 
 }  // namespace hdb

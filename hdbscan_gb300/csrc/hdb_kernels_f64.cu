@@ -1,20 +1,28 @@
-// float64 kernel variants.  Register budget: V*DP doubles of coordinates per
-// thread stay <= 16 at 1024 threads and <= 32 below.
+// float64 kernel variants.  Register budget: SV*DP doubles of coordinates per
+// Prim thread stay <= 32 (64 registers).
 #include "hdb_instances.cuh"
 
 namespace hdb {
 namespace {
 const ForwardVariant kForward[] = {
-    forward_variant<double, 128, 1, 8>(),  forward_variant<double, 128, 1, 16>(),
-    forward_variant<double, 128, 1, 0>(),
-    forward_variant<double, 256, 1, 8>(),  forward_variant<double, 256, 1, 16>(),
-    forward_variant<double, 256, 1, 0>(),
-    forward_variant<double, 512, 1, 8>(),  forward_variant<double, 512, 1, 16>(),
-    forward_variant<double, 512, 1, 0>(),
-    forward_variant<double, 512, 2, 8>(),  forward_variant<double, 512, 2, 16>(),
+    forward_variant<double, 32, 2, 8>(),
+    forward_variant<double, 32, 2, 16>(),
+    forward_variant<double, 32, 2, 0>(),
+    forward_variant<double, 64, 2, 8>(),
+    forward_variant<double, 64, 2, 16>(),
+    forward_variant<double, 64, 2, 0>(),
+    forward_variant<double, 128, 2, 8>(),
+    forward_variant<double, 128, 2, 16>(),
+    forward_variant<double, 128, 2, 0>(),
+    forward_variant<double, 256, 2, 8>(),
+    forward_variant<double, 256, 2, 16>(),
+    forward_variant<double, 256, 2, 0>(),
+    forward_variant<double, 512, 2, 8>(),
+    forward_variant<double, 512, 2, 16>(),
     forward_variant<double, 512, 2, 0>(),
-    forward_variant<double, 1024, 2, 8>(), forward_variant<double, 1024, 2, 0>(),
-    forward_variant<double, 1024, 4, 0>(),
+    forward_variant<double, 512, 4, 8>(),
+    forward_variant<double, 512, 4, 0>(),
+    forward_variant<double, 512, 8, 0>(),
 };
 const CoreVariant kCore[] = {
     core_points_variant<double, 8, 8>(),   core_points_variant<double, 8, 16>(),
@@ -31,7 +39,7 @@ const CoreVariant kCore[] = {
 const PrecisionKernels kTable = {
     8, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), kCore, (int)(sizeof(kCore) / sizeof(kCore[0])),
     launch_distance<double>, launch_select<double>, (const void*)hdb_core_select_kernel<double>,
-    launch_backward<double>, forward_smem_dispatch<double>,
+    launch_backward<double>, forward_layout<double>,
 };
 }  // namespace
 const PrecisionKernels& kernels_f64() { return kTable; }

@@ -94,14 +94,16 @@ __global__ void noalloc_tables_kernel(int64_t* offsets, int32_t* queue, int32_t*
 
 const hdb::ForwardVariant* pick_forward(const hdb::PrecisionKernels& k, int precision, int n, int dims) {
     int threads, v;
-    if (n <= 128) { threads = 128; v = 1; }
-    else if (n <= 256) { threads = 256; v = 1; }
-    else if (n <= 512) { threads = 512; v = 1; }
+    if (n <= 64) { threads = 32; v = 2; }
+    else if (n <= 128) { threads = 64; v = 2; }
+    else if (n <= 256) { threads = 128; v = 2; }
+    else if (n <= 512) { threads = 256; v = 2; }
     else if (n <= 1024) { threads = 512; v = 2; }
-    else if (n <= 2048) { threads = 1024; v = 2; }
-    else { threads = 1024; v = 4; }
+    else if (n <= 2048) { threads = 512; v = 4; }
+    else { threads = 512; v = 8; }
+    const int words = precision == HDB_F32 ? 1 : 2;
     for (int dp : {8, 16, 32}) {
-        if (dims > dp || (precision == HDB_F64 && dp > 16)) continue;
+        if (dims > dp || v * dp * words > 64) continue;
         for (int i = 0; i < k.n_forward; ++i)
             if (k.forward[i].threads == threads && k.forward[i].v == v && k.forward[i].dp == dp) return &k.forward[i];
     }
@@ -164,12 +166,17 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
-    int xs = 1;
-    size_t smem = k.forward_smem(n, fv->dp, true, unit);
-    if (smem > (size_t)optin - 2048) { xs = 0; smem = k.forward_smem(n, fv->dp, false, unit); }
+    cudaFuncAttributes attr;
+    e = cudaFuncGetAttributes(&attr, fv->func);
+    if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
+    const size_t budget = (size_t)optin > attr.sharedSizeBytes + 1024 ? (size_t)optin - attr.sharedSizeBytes - 1024 : 0;
+    hdb::ForwardLayout layout{};
+    if (!k.forward_layout(n, fv->dp, unit, budget, &layout))
+        return fail(HDB_E_INVALID, "window exceeds shared memory");
+    const size_t smem = layout.bytes;
     e = hdb::raise_dynamic_smem(fv->func, smem);
     int per_sm = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fv->func, fv->threads, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fv->func, fv->threads + 32, smem);
     if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("forward kernel set-up: ") + cudaGetErrorString(e));
     if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
     const size_t select_smem = (size_t)n * (precision == HDB_F32 ? 4 : 8);
@@ -217,7 +224,11 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     a.D = dims;
     a.mcs = min_cluster_size;
     a.unit_core = unit ? 1 : 0;
-    a.x_in_smem = xs;
+    a.x_in_smem = layout.x_in_smem;
+    a.n_arenas = layout.n_arenas;
+    a.arena_stride = (int)layout.arena_stride;
+    a.x_off = (int)layout.x_off;
+    a.core_off = (int)layout.core_off;
     a.eps = epsilon;
     a.core = unit ? nullptr : core;
     a.labels = labels;

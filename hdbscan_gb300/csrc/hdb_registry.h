@@ -9,9 +9,19 @@
 
 namespace hdb {
 
+// Dynamic shared-memory layout of one forward launch.
+struct ForwardLayout {
+    int n_arenas;
+    int x_in_smem;
+    size_t arena_stride;
+    size_t x_off;
+    size_t core_off;
+    size_t bytes;
+};
+
 struct ForwardVariant {
-    int threads;
-    int v;        // vertices per thread
+    int threads;  // Prim threads; the CTA has threads + 32 (one tree warp)
+    int v;        // vertices (slots) per Prim thread
     int dp;       // padded register dimensions; 0 = matrix variant
     const void* func;
     void (*launch)(const ForwardArgs&, int grid, size_t smem, cudaStream_t);
@@ -34,7 +44,8 @@ struct PrecisionKernels {
     void (*launch_select)(const CoreArgs&, int grid, size_t smem, cudaStream_t);
     const void* select_func;
     void (*launch_backward)(const BackwardArgs&, int grid, cudaStream_t);
-    size_t (*forward_smem)(int n, int dp, bool x_in_smem, bool unit_core);
+    // Best layout for windows of up to n points within `budget` bytes; false if none fits.
+    bool (*forward_layout)(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out);
 };
 
 const PrecisionKernels& kernels_f32();

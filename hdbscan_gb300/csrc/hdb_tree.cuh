@@ -1,36 +1,51 @@
-// Hierarchy stages of one window, run by one CTA on a shared-memory arena:
-// indirect introsort -> union-find single linkage -> breadth-first
-// condensation -> excess-of-mass selection -> epsilon merge -> labels.
+// Hierarchy stages of one window, run by ONE warp (the tree warp of the
+// forward kernel) on a shared-memory arena: exact NumPy-order introsort ->
+// union-find single linkage -> breadth-first condensation -> excess of mass
+// -> epsilon merge -> labels.
 //
 // Semantics follow the reference kernels (hdbscan_gpu/_kernels.py) stage by
-// stage; each function cites the lines it reproduces.  The arena layout and
-// the lifetime aliasing below are this project's own (16-bit indices, sort on
-// (weight, index) pairs so each compare is one shared-memory load, endpoints
-// gathered into sorted order before linkage).
+// stage; each function cites the lines it reproduces.  The parallel
+// decompositions are this project's own:
+//  * the introsort runs every Hoare partition warp-parallel.  For a segment
+//    whose pivot sits at hi-1, let A be the ascending positions in
+//    [lo+1, hi-1] holding w >= pivot (where the i scan stops) and B the
+//    descending positions in [lo, hi-2] holding w <= pivot (where the j scan
+//    stops).  The serial loop swaps A[k] with B[k] exactly while A[k] < B[k],
+//    i.e. an A-stopper of rank k swaps iff more than k B-stoppers lie to its
+//    right (and symmetrically for B), and stops at i = min(A[K], B[K-1]) for
+//    K swaps.  Ranks come from ballots, so each partition is two passes over
+//    the segment plus K/32 swap rounds, with NumPy's exact swap sequence.
+//    Segments of <= 16 elements and depth-exhausted heapsort segments are
+//    finished one per lane.
+//  * linkage uses union by size over packed 64-bit words
+//    (parent | component node << 16 | size << 32) without path compression;
+//    the roots, hence the tree, are those of the reference's union-find.
+//  * selection uses the binary shape of the condensed tree (every split
+//    creates exactly two consecutive ids), as the reference's
+//    COOPERATIVE_BINARY_EOM variant does (_kernels.py:648-669).
 #pragma once
 #include "hdb_common.cuh"
 
 namespace hdb {
 
-// Element of the sort: the weight and the Prim edge index travel together.
 template <typename Real> struct SortPair;
 template <> struct __align__(8) SortPair<float> { float w; int32_t idx; };
 template <> struct __align__(16) SortPair<double> { double w; int64_t idx; };
 
 // Shared-memory arena for one window of capacity `cap` points (cap >= n).
-//  r0  Real[cap]  edge weights in Prim order -> weights in sorted order
-//  r1  Real[cap]  cluster birth lambda        (r1+r2 = SortPair[cap] during the sort)
-//  r2  Real[cap]  cluster stability
-//  s0  i16[cap]   Prim edge source            -> prune queue [0, cap)
-//  s1  i16[cap]   Prim edge new vertex        -> prune queue [cap, 2cap)
-//  s2  i16[cap]   sorted edge order           -> sorted sources
-//  s3  i16[cap]   sort tasks | linkage left   -> first child
-//  s4  i16[cap]   sort tasks | linkage right  -> next sibling
-//  s5  i16[cap]   sort tasks | linkage size   -> EOM blocked -> epsilon stop
-//  s6  i16[cap]   sort tasks | union-find     -> relabel -> resolved label
-//  s7  i16[cap]   sort tasks | component node -> BFS queue -> label map
-//  s8  i16[cap]   sort tasks | sorted targets -> cluster parent
-//  s9  i16[cap]   point parent
+//  r0  Real[cap]  Prim edge weights -> weights in sorted order (merge weights)
+//  r1  Real[cap]  \  SortPair[cap] during the sort -> union-find words during
+//  r2  Real[cap]  /  linkage -> cluster birth (r1) and stability (r2)
+//  s0  i16[cap]   Prim edge source  -> prune queue [0, cap)
+//  s1  i16[cap]   Prim edge target  -> prune queue [cap, 2cap)
+//  s2  i16[cap]   sorted order -> sorted sources -> cluster parent
+//  s3  i16[cap]   sort swap list A -> sorted targets -> first child
+//  s4  i16[cap]   sort swap list B -> linkage left -> EOM blocked
+//  s5  i16[cap]   task lo -> linkage right -> epsilon stop
+//  s6  i16[cap]   task hi -> linkage size -> label map
+//  s7  i16[cap]   task depth -> relabel -> resolved label
+//  s8  i16[cap]   leaf lo -> BFS queue
+//  s9  i16[cap]   leaf hi -> point parent
 //  sel u8[cap]    cluster selected flag
 template <typename Real> struct Arena {
     Real *r0, *r1, *r2;
@@ -40,7 +55,7 @@ template <typename Real> struct Arena {
     __host__ __device__ static int round_cap(int n) { return (n + 7) & ~7; }
     __host__ __device__ static size_t bytes(int n) {
         const size_t cap = (size_t)round_cap(n);
-        return 3 * cap * sizeof(Real) + 10 * cap * sizeof(int16_t) + cap;
+        return (3 * cap * sizeof(Real) + 10 * cap * sizeof(int16_t) + cap + 15) & ~size_t(15);
     }
     __device__ static Arena carve(void* base, int n) {
         Arena a;
@@ -57,12 +72,14 @@ template <typename Real> struct Arena {
     }
 };
 
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
 // ---------------------------------------------------------------------------
-// Indirect introsort (reference: _kernels.py:358-516; NumPy 2.3.5 scalar
-// aquicksort semantics).  Tie order depends on the exact sequence of
-// median-of-3 swaps, Hoare partition swaps, insertion shifts and heapsort
-// moves, so each task runs them serially; independent tasks run in parallel
-// threads exactly as the reference's PARALLEL_SORT rounds (:441-480).
+// Introsort (reference: _kernels.py:358-516; NumPy 2.3.5 aquicksort).
 // ---------------------------------------------------------------------------
 template <typename Real>
 __device__ void heap_sort_pairs(SortPair<Real>* p, int lo, int hi) {
@@ -91,42 +108,7 @@ __device__ void heap_sort_pairs(SortPair<Real>* p, int lo, int hi) {
 }
 
 template <typename Real>
-__device__ __forceinline__ void swap_pairs(SortPair<Real>* p, int i, int j) {
-    SortPair<Real> t = p[i]; p[i] = p[j]; p[j] = t;
-}
-
-// Runs one task: heapsort if its (checked) depth is exhausted, else partition
-// until <= 16 elements, deferring the larger side into `next_*`.
-template <typename Real>
-__device__ void sort_task(SortPair<Real>* p, int lo, int hi, int depth,
-                          int16_t* next_lo, int16_t* next_hi, int16_t* next_depth, int* pending) {
-    if (depth < 0) { heap_sort_pairs(p, lo, hi); return; }
-    while (hi - lo > 15) {
-        const int mid = lo + ((hi - lo) >> 1);
-        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
-        if (p[hi].w < p[mid].w) swap_pairs(p, hi, mid);
-        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
-        const Real pivot = p[mid].w;
-        int i = lo, j = hi - 1;
-        swap_pairs(p, mid, j);
-        for (;;) {
-            do { ++i; } while (p[i].w < pivot);
-            do { --j; } while (pivot < p[j].w);
-            if (i >= j) break;
-            swap_pairs(p, i, j);
-        }
-        swap_pairs(p, i, hi - 1);
-        --depth;
-        const int slot = atomicAdd(pending, 1);
-        if (i - lo < hi - i) {
-            next_lo[slot] = (int16_t)(i + 1); next_hi[slot] = (int16_t)hi;
-            hi = i - 1;
-        } else {
-            next_lo[slot] = (int16_t)lo; next_hi[slot] = (int16_t)(i - 1);
-            lo = i + 1;
-        }
-        next_depth[slot] = (int16_t)depth;
-    }
+__device__ void insertion_sort_pairs(SortPair<Real>* p, int lo, int hi) {
     for (int i = lo + 1; i <= hi; ++i) {
         SortPair<Real> value = p[i];
         int j = i;
@@ -135,206 +117,329 @@ __device__ void sort_task(SortPair<Real>* p, int lo, int hi, int depth,
     }
 }
 
-// Sorts r0[0..m) (m = n-1 edge weights) into pairs; leaves the order in s2
-// and the sorted weights in r0.  Whole-CTA call.
 template <typename Real>
-__device__ void sort_edges(const Arena<Real>& a, int m, int* s_counter) {
+__device__ __forceinline__ void swap_pairs(SortPair<Real>* p, int i, int j) {
+    SortPair<Real> t = p[i]; p[i] = p[j]; p[j] = t;
+}
+
+// One Hoare partition of p[lo..hi] (hi - lo > 15) by the whole warp.
+// Returns the pivot's final position (warp-uniform).
+template <typename Real>
+__device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a, int16_t* list_b) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        const int mid = lo + ((hi - lo) >> 1);
+        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
+        if (p[hi].w < p[mid].w) swap_pairs(p, hi, mid);
+        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
+        swap_pairs(p, mid, hi - 1);
+    }
+    __syncwarp();
+    const Real pivot = p[hi - 1].w;
+    // Pass 1: stopper totals.
+    int total_a = 0, total_b = 0;
+    for (int base = lo; base <= hi - 1; base += 32) {
+        const int pos = base + lane;
+        bool fa = false, fb = false;
+        if (pos <= hi - 1) {
+            const Real w = p[pos].w;
+            fa = pos >= lo + 1 && !(w < pivot);
+            fb = pos <= hi - 2 && !(pivot < w);
+        }
+        total_a += __popc(__ballot_sync(0xffffffffu, fa));
+        total_b += __popc(__ballot_sync(0xffffffffu, fb));
+    }
+    // Pass 2: ranks, swap decisions, swap lists, first non-swapping A.
+    int run_a = 0, run_b = 0, swaps = 0, first_stop = -1;
+    const unsigned lt = lanemask_lt();
+    for (int base = lo; base <= hi - 1; base += 32) {
+        const int pos = base + lane;
+        bool fa = false, fb = false;
+        if (pos <= hi - 1) {
+            const Real w = p[pos].w;
+            fa = pos >= lo + 1 && !(w < pivot);
+            fb = pos <= hi - 2 && !(pivot < w);
+        }
+        const unsigned ba = __ballot_sync(0xffffffffu, fa);
+        const unsigned bb = __ballot_sync(0xffffffffu, fb);
+        const int a_before = run_a + __popc(ba & lt);          // A-stoppers left of pos
+        const int b_upto = run_b + __popc(bb & (lt | (1u << lane)));
+        const int b_after = total_b - b_upto;                   // B-stoppers right of pos
+        const bool swap_a = fa && b_after > a_before;
+        const bool swap_b = fb && a_before > b_after;
+        if (swap_a) list_a[lo + a_before] = (int16_t)pos;
+        if (swap_b) list_b[lo + b_after] = (int16_t)pos;
+        swaps += __popc(__ballot_sync(0xffffffffu, swap_a));
+        const unsigned stop = __ballot_sync(0xffffffffu, fa && !swap_a);
+        if (first_stop < 0 && stop) first_stop = base + __ffs(stop) - 1;
+        run_a += __popc(ba);
+        run_b += __popc(bb);
+    }
+    __syncwarp();
+    for (int k = lane; k < swaps; k += 32) swap_pairs(p, list_a[lo + k], list_b[lo + k]);
+    __syncwarp();
+    int i = first_stop;
+    if (swaps > 0) {
+        const int last_b = list_b[lo + swaps - 1];
+        i = last_b < i ? last_b : i;
+    }
+    if (lane == 0) swap_pairs(p, i, hi - 1);
+    __syncwarp();
+    return i;
+}
+
+// Sorts r0[0..m) with NumPy's quicksort order; leaves the order in s2 and the
+// sorted weights in r0.  Whole-warp call.
+template <typename Real>
+__device__ void sort_edges_warp(const Arena<Real>& a, int m) {
+    const int lane = threadIdx.x & 31;
     SortPair<Real>* p = reinterpret_cast<SortPair<Real>*>(a.r1);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) { p[i].w = a.r0[i]; p[i].idx = i; }
-    int16_t *cur_lo = a.s3, *cur_hi = a.s4, *cur_depth = a.s5;
-    int16_t *nxt_lo = a.s6, *nxt_hi = a.s7, *nxt_depth = a.s8;
-    __shared__ int s_tasks;
-    if (threadIdx.x == 0) {
+    for (int i = lane; i < m; i += 32) { p[i].w = a.r0[i]; p[i].idx = i; }
+    int16_t *task_lo = a.s5, *task_hi = a.s6, *task_depth = a.s7;  // depth*2 + checked
+    int16_t *leaf_lo = a.s8, *leaf_hi = a.s9;                        // hi < 0: heapsort ~hi
+    int top = 0, leaves = 0;
+    if (m > 1) {
         int depth = 0;
         for (int c = m; c > 1; c >>= 1) depth += 2;  // 2*floor(log2(m)), _kernels.py:429-431
-        s_tasks = m > 1 ? 1 : 0;
-        cur_lo[0] = 0; cur_hi[0] = (int16_t)(m - 1); cur_depth[0] = (int16_t)depth;
-        *s_counter = 0;
+        if (lane == 0) { task_lo[0] = 0; task_hi[0] = (int16_t)(m - 1); task_depth[0] = (int16_t)(depth * 2 + 1); }
+        top = 1;
     }
-    __syncthreads();
-    int rounds = 0;
-    while (s_tasks > 0 && rounds < 4 * 32768) {
-        const int tasks = s_tasks;
-        for (int t = threadIdx.x; t < tasks; t += blockDim.x)
-            sort_task(p, cur_lo[t], cur_hi[t], cur_depth[t], nxt_lo, nxt_hi, nxt_depth, s_counter);
-        __syncthreads();
-        if (threadIdx.x == 0) { s_tasks = *s_counter; *s_counter = 0; }
-        __syncthreads();
-        int16_t* t0 = cur_lo; cur_lo = nxt_lo; nxt_lo = t0;
-        t0 = cur_hi; cur_hi = nxt_hi; nxt_hi = t0;
-        t0 = cur_depth; cur_depth = nxt_depth; nxt_depth = t0;
-        ++rounds;
+    __syncwarp();
+    while (top > 0) {
+        --top;
+        const int lo = task_lo[top], hi = task_hi[top], code = task_depth[top];
+        const int depth = code >> 1;  // arithmetic shift keeps negative depths
+        const bool checked = code & 1;
+        __syncwarp();
+        if (checked && depth < 0) {
+            // Popped task with exhausted depth: heapsort (reference :442-443).
+            if (lane == 0) { leaf_lo[leaves] = (int16_t)lo; leaf_hi[leaves] = (int16_t)~hi; }
+            ++leaves;
+        } else if (hi - lo <= 15) {
+            if (lane == 0) { leaf_lo[leaves] = (int16_t)lo; leaf_hi[leaves] = (int16_t)hi; }
+            ++leaves;
+        } else {
+            const int i = partition_warp(p, lo, hi, a.s3, a.s4);
+            const int d = depth - 1;
+            // The larger side is deferred (checked on pop); the smaller side
+            // continues in place without a depth check (_kernels.py:449-462).
+            int big_lo, big_hi, small_lo, small_hi;
+            if (i - lo < hi - i) { big_lo = i + 1; big_hi = hi; small_lo = lo; small_hi = i - 1; }
+            else { big_lo = lo; big_hi = i - 1; small_lo = i + 1; small_hi = hi; }
+            if (lane == 0) {
+                task_lo[top] = (int16_t)big_lo; task_hi[top] = (int16_t)big_hi; task_depth[top] = (int16_t)(d * 2 + 1);
+                task_lo[top + 1] = (int16_t)small_lo; task_hi[top + 1] = (int16_t)small_hi;
+                task_depth[top + 1] = (int16_t)(d * 2);
+            }
+            top += 2;
+        }
+        __syncwarp();
     }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    for (int t = lane; t < leaves; t += 32) {
+        const int lo = leaf_lo[t], hi = leaf_hi[t];
+        if (hi < 0) heap_sort_pairs(p, lo, ~hi);
+        else insertion_sort_pairs(p, lo, hi);
+    }
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
         a.s2[i] = (int16_t)p[i].idx;
         a.r0[i] = p[i].w;
     }
-    __syncthreads();
+    __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
-// Single linkage (reference: _kernels.py:518-556, scikit-learn
-// make_single_linkage semantics).  Node n+i merges the components of the
-// i-th sorted edge's (source, target), children oriented (source side,
-// target side).  Balanced union-find over leaf representatives with path
-// halving; the component's current dendrogram node is kept per representative.
-// Serial (thread 0).  Inputs: s2 = sorted sources, s8 = sorted targets.
-// Outputs: s3 left, s4 right, s5 size for node n+i at index i.
+// Single linkage (reference: _kernels.py:518-556).  Node n+i merges the
+// components of the i-th sorted edge (source side first).  Inputs: s2 sorted
+// sources, s3 sorted targets.  Outputs: s4 left, s5 right, s6 size of node n+i
+// at index i.  Lane 0 runs the union-find; the words live in r1/r2.
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ void linkage_serial(const Arena<Real>& a, int n) {
-    int16_t* uf = a.s6;
-    int16_t* comp = a.s7;
-    for (int i = 0; i < n - 1; ++i) {
-        int x = a.s2[i], y = a.s8[i];
-        int px = uf[x];
-        while (px != x) { const int g = uf[px]; uf[x] = (int16_t)g; x = g; px = uf[x]; }
-        int py = uf[y];
-        while (py != y) { const int g = uf[py]; uf[y] = (int16_t)g; y = g; py = uf[y]; }
-        const int ca = comp[x], cc = comp[y];
-        const int sa = ca < n ? 1 : a.s5[ca - n];
-        const int sc = cc < n ? 1 : a.s5[cc - n];
-        a.s3[i] = (int16_t)ca;
-        a.s4[i] = (int16_t)cc;
-        a.s5[i] = (int16_t)(sa + sc);
-        if (sa < sc) { uf[x] = (int16_t)y; comp[y] = (int16_t)(n + i); }
-        else { uf[y] = (int16_t)x; comp[x] = (int16_t)(n + i); }
+__device__ void linkage_warp(const Arena<Real>& a, int n) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long* U = reinterpret_cast<unsigned long long*>(a.r1);
+    for (int x = lane; x < n; x += 32)
+        U[x] = (unsigned long long)x | ((unsigned long long)x << 16) | (1ull << 32);
+    __syncwarp();
+    if (lane == 0) {
+        for (int i = 0; i < n - 1; ++i) {
+            int x = a.s2[i], y = a.s3[i];
+            unsigned long long wx = U[x], wy = U[y];
+            while ((int)(wx & 0xffff) != x) { x = (int)(wx & 0xffff); wx = U[x]; }
+            while ((int)(wy & 0xffff) != y) { y = (int)(wy & 0xffff); wy = U[y]; }
+            const unsigned long long sx = wx >> 32, sy = wy >> 32, s = sx + sy;
+            a.s4[i] = (int16_t)((wx >> 16) & 0xffff);
+            a.s5[i] = (int16_t)((wy >> 16) & 0xffff);
+            a.s6[i] = (int16_t)s;
+            const unsigned long long node = (unsigned long long)(n + i) << 16;
+            if (sx < sy) {
+                U[x] = (wx & ~0xffffull) | (unsigned long long)y;
+                U[y] = (unsigned long long)y | node | (s << 32);
+            } else {
+                U[y] = (wy & ~0xffffull) | (unsigned long long)x;
+                U[x] = (unsigned long long)x | node | (s << 32);
+            }
+        }
     }
+    __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
-// Breadth-first condensation (reference: _kernels.py:558-643).  Serial.
-// Linkage node ids are n..2n-2 (index id-n); cluster ids are n.. (index id-n).
-// Returns next_label.
+// Breadth-first condensation (reference: _kernels.py:558-643).  Lane 0 runs
+// the queue; lanes initialise.  Linkage node ids n..2n-2 (index id-n); cluster
+// ids n.. (index id-n).  Returns next_label (warp-uniform).
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ int condense_serial(const Arena<Real>& a, int n, int mcs) {
-    int16_t* relabel = a.s6;   // per linkage node
-    int16_t* queue = a.s7;     // linkage nodes (ids)
-    int16_t* prune = a.s0;     // 2*cap entries across s0,s1
-    int16_t* parent = a.s8;    // per cluster
+__device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
+    const int lane = threadIdx.x & 31;
+    int16_t* relabel = a.s7;
+    int16_t* queue = a.s8;
+    int16_t* prune = a.s0;   // 2*cap entries across s0,s1
+    int16_t* parent = a.s2;
     Real* birth = a.r1;
     Real* stab = a.r2;
+    const int16_t* left = a.s4;
+    const int16_t* right = a.s5;
+    const int16_t* size = a.s6;
     const Real inf = RealTraits<Real>::inf();
-    for (int c = 0; c < n; ++c) { parent[c] = -1; birth[c] = 0; stab[c] = 0; a.sel[c] = 0; }
-    const int root = 2 * n - 2;
-    int head = 0, tail = 1, next_label = n + 1;
-    queue[0] = (int16_t)root;
-    relabel[root - n] = (int16_t)n;
-    while (head < tail) {
-        const int node = queue[head++];
-        const int ni = node - n;
-        const int left = a.s3[ni], right = a.s4[ni];
-        const int cluster = relabel[ni];
-        const int ci = cluster - n;
-        const Real cluster_birth = birth[ci];
-        Real cluster_stability = stab[ci];
-        const Real dist = a.r0[ni];
-        const Real lambda = dist > Real(0) ? RealTraits<Real>::recip(dist) : inf;
-        const int size_l = left < n ? 1 : a.s5[left - n];
-        const int size_r = right < n ? 1 : a.s5[right - n];
-        const bool large_l = size_l >= mcs, large_r = size_r >= mcs;
-        if (large_l && large_r) {
-            // Both children: new consecutive ids (_kernels.py:603-613).
-            for (int k = 0; k < 2; ++k) {
-                const int child = k == 0 ? left : right;
-                const int size = k == 0 ? size_l : size_r;
-                const int label = next_label++;
-                relabel[child - n] = (int16_t)label;
-                parent[label - n] = (int16_t)cluster;
-                birth[label - n] = lambda;
-                a.sel[label - n] = 1;
-                cluster_stability = RealTraits<Real>::add(
-                    cluster_stability,
-                    RealTraits<Real>::mul(RealTraits<Real>::sub(lambda, cluster_birth), (Real)size));
-                queue[tail++] = (int16_t)child;
-            }
-        } else {
-            for (int k = 0; k < 2; ++k) {
-                const int child = k == 0 ? left : right;
-                if (k == 0 ? large_l : large_r) {
-                    relabel[child - n] = (int16_t)cluster;
+    for (int c = lane; c < n; c += 32) { parent[c] = -1; birth[c] = 0; stab[c] = 0; a.sel[c] = 0; }
+    __syncwarp();
+    int next_label = n + 1;
+    if (lane == 0) {
+        const int root = 2 * n - 2;
+        int head = 0, tail = 1;
+        queue[0] = (int16_t)root;
+        relabel[root - n] = (int16_t)n;
+        while (head < tail) {
+            const int node = queue[head++];
+            const int ni = node - n;
+            const int l = left[ni], r = right[ni];
+            const int cluster = relabel[ni];
+            const int ci = cluster - n;
+            const Real cluster_birth = birth[ci];
+            Real cluster_stability = stab[ci];
+            const Real dist = a.r0[ni];
+            const Real lambda = dist > Real(0) ? RealTraits<Real>::recip(dist) : inf;
+            const int size_l = l < n ? 1 : size[l - n];
+            const int size_r = r < n ? 1 : size[r - n];
+            const bool large_l = size_l >= mcs, large_r = size_r >= mcs;
+            if (large_l && large_r) {
+                // Both children: new consecutive ids (_kernels.py:603-613).
+                for (int k = 0; k < 2; ++k) {
+                    const int child = k == 0 ? l : r;
+                    const int csize = k == 0 ? size_l : size_r;
+                    const int label = next_label++;
+                    relabel[child - n] = (int16_t)label;
+                    parent[label - n] = (int16_t)cluster;
+                    birth[label - n] = lambda;
+                    a.sel[label - n] = 1;
+                    cluster_stability = RealTraits<Real>::add(
+                        cluster_stability,
+                        RealTraits<Real>::mul(RealTraits<Real>::sub(lambda, cluster_birth), (Real)csize));
                     queue[tail++] = (int16_t)child;
-                } else {
-                    // Prune the whole subtree leaf by leaf (_kernels.py:626-637).
-                    const Real term = RealTraits<Real>::sub(lambda, cluster_birth);
-                    int ph = 0, pt = 0, leaf = child;
-                    for (;;) {
-                        if (leaf < n) {
-                            a.s9[leaf] = (int16_t)cluster;
+                }
+            } else {
+                for (int k = 0; k < 2; ++k) {
+                    const int child = k == 0 ? l : r;
+                    if (k == 0 ? large_l : large_r) {
+                        relabel[child - n] = (int16_t)cluster;
+                        queue[tail++] = (int16_t)child;
+                    } else {
+                        // Prune the whole subtree leaf by leaf (_kernels.py:626-637);
+                        // every leaf adds the same term, so only the count matters.
+                        const Real term = RealTraits<Real>::sub(lambda, cluster_birth);
+                        if (child < n) {
+                            a.s9[child] = (int16_t)cluster;
                             cluster_stability = RealTraits<Real>::add(cluster_stability, term);
                         } else {
-                            prune[pt++] = a.s3[leaf - n];
-                            prune[pt++] = a.s4[leaf - n];
+                            int ph = 0, pt = 0, leaf = child;
+                            for (;;) {
+                                if (leaf < n) {
+                                    a.s9[leaf] = (int16_t)cluster;
+                                    cluster_stability = RealTraits<Real>::add(cluster_stability, term);
+                                } else {
+                                    prune[pt++] = left[leaf - n];
+                                    prune[pt++] = right[leaf - n];
+                                }
+                                if (ph == pt) break;
+                                leaf = prune[ph++];
+                            }
                         }
-                        if (ph == pt) break;
-                        leaf = prune[ph++];
                     }
                 }
             }
+            stab[ci] = cluster_stability;
         }
-        stab[ci] = cluster_stability;
     }
+    next_label = __shfl_sync(0xffffffffu, next_label, 0);
+    __syncwarp();
     return next_label;
 }
 
 // ---------------------------------------------------------------------------
-// Excess of mass (reference: _kernels.py:672-710) + epsilon and labels
-// (reference: _kernels.py:712-760).  Serial; writes labels[0..n).
+// Excess of mass (reference: _kernels.py:672-710, binary form :648-669) and
+// epsilon merge + labels (reference: _kernels.py:712-760).  Writes
+// labels[0..n) through `labels` (global memory).
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ void select_and_label(const Arena<Real>& a, int n, int next_label, Real epsilon, int32_t* labels) {
+__device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_label, Real epsilon,
+                                      int32_t* labels) {
+    const int lane = threadIdx.x & 31;
     const int clusters = next_label - n;
-    int16_t* parent = a.s8;
-    Real* birth = a.r1;
+    const int16_t* parent = a.s2;
+    const Real* birth = a.r1;
     Real* stab = a.r2;
-    int16_t* first_child = a.s3;
-    int16_t* next_sibling = a.s4;
-    for (int c = 0; c < clusters; ++c) { first_child[c] = -1; next_sibling[c] = -1; }
-    // Descending insertion keeps children in ascending id order.
-    for (int child = next_label - 1; child > n; --child) {
-        const int anc = parent[child - n] - n;
-        next_sibling[child - n] = first_child[anc];
-        first_child[anc] = (int16_t)child;
-    }
-    for (int node = next_label - 1; node > n; --node) {
-        Real subtree = 0;
-        for (int child = first_child[node - n]; child != -1; child = next_sibling[child - n])
-            subtree = RealTraits<Real>::add(subtree, stab[child - n]);
-        if (subtree > stab[node - n]) {
-            a.sel[node - n] = 0;
-            stab[node - n] = subtree;
+    int16_t* first = a.s3;
+    for (int c = lane; c < clusters; c += 32) first[c] = -1;
+    __syncwarp();
+    // Children come in consecutive pairs (n+1, n+2), (n+3, n+4), ...
+    for (int child = n + 1 + 2 * lane; child < next_label; child += 64) first[parent[child - n] - n] = (int16_t)child;
+    __syncwarp();
+    if (lane == 0) {
+        for (int node = next_label - 1; node > n; --node) {
+            const int f = first[node - n];
+            const Real subtree = f < 0 ? Real(0)
+                                       : RealTraits<Real>::add(RealTraits<Real>::add(Real(0), stab[f - n]),
+                                                               stab[f + 1 - n]);
+            if (subtree > stab[node - n]) {
+                a.sel[node - n] = 0;
+                stab[node - n] = subtree;
+            }
         }
-    }
-    int16_t* blocked = a.s5;
-    blocked[0] = 0;
-    for (int node = n + 1; node < next_label; ++node) {
-        const int inherited = blocked[parent[node - n] - n];
-        blocked[node - n] = (int16_t)(inherited || a.sel[node - n]);
-        if (inherited) a.sel[node - n] = 0;
-    }
-    int16_t* label_map = a.s7;
-    for (int c = 0; c < clusters; ++c) label_map[c] = -1;
-    if (epsilon > Real(0)) {
-        int16_t* stop = a.s5;  // blocked is dead
+        // Parents have smaller ids: one forward pass suppresses descendants.
+        int16_t* blocked = a.s4;
+        blocked[0] = 0;
         for (int node = n + 1; node < next_label; ++node) {
-            const int anc = parent[node - n];
-            stop[node - n] = (int16_t)(anc == n ? node
-                                                : (RealTraits<Real>::recip(birth[anc - n]) > epsilon ? anc : stop[anc - n]));
-            if (!a.sel[node - n]) continue;
-            const int chosen = RealTraits<Real>::recip(birth[node - n]) < epsilon ? stop[node - n] : node;
-            label_map[chosen - n] = 1;
+            const int inherited = blocked[parent[node - n] - n];
+            blocked[node - n] = (int16_t)(inherited || a.sel[node - n]);
+            if (inherited) a.sel[node - n] = 0;
         }
-        for (int node = n + 1; node < next_label; ++node) a.sel[node - n] = label_map[node - n] == 1;
+        int16_t* label_map = a.s6;
+        for (int c = 0; c < clusters; ++c) label_map[c] = -1;
+        if (epsilon > Real(0)) {
+            int16_t* stop = a.s5;
+            for (int node = n + 1; node < next_label; ++node) {
+                const int anc = parent[node - n];
+                stop[node - n] = (int16_t)(anc == n ? node
+                                                    : (RealTraits<Real>::recip(birth[anc - n]) > epsilon ? anc
+                                                                                                         : stop[anc - n]));
+                if (!a.sel[node - n]) continue;
+                const int chosen = RealTraits<Real>::recip(birth[node - n]) < epsilon ? stop[node - n] : node;
+                label_map[chosen - n] = 1;
+            }
+            for (int node = n + 1; node < next_label; ++node) a.sel[node - n] = label_map[node - n] == 1;
+        }
+        int label = 0;
+        for (int node = n + 1; node < next_label; ++node)
+            if (a.sel[node - n]) label_map[node - n] = (int16_t)label++;
+        int16_t* resolved = a.s7;
+        resolved[0] = -1;
+        for (int node = n + 1; node < next_label; ++node)
+            resolved[node - n] = a.sel[node - n] ? label_map[node - n] : resolved[parent[node - n] - n];
     }
-    int label = 0;
-    for (int node = n + 1; node < next_label; ++node)
-        if (a.sel[node - n]) label_map[node - n] = (int16_t)label++;
-    int16_t* resolved = a.s6;
-    resolved[0] = -1;
-    for (int node = n + 1; node < next_label; ++node)
-        resolved[node - n] = a.sel[node - n] ? label_map[node - n] : resolved[parent[node - n] - n];
-    (void)labels;
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) labels[i] = a.s7[a.s9[i] - n];
+    __syncwarp();
 }
 
 }  // namespace hdb
