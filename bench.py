@@ -278,12 +278,12 @@ def main():
         plan.forward(X, labels=labels, workspace=workspace, status=status, exports={"stage_ns": stamps})
         torch.cuda.synchronize()
         st = stamps.cpu().numpy().astype(np.float64)
-        names = ["stage", "prim", "sort", "linkage", "condense", "select_label"]
-        dur = np.diff(st[:, :7], axis=1) / 1e3
+        names = ["stage", "prim", "handoff_wait", "sort", "linkage", "condense", "select_label"]
+        dur = np.diff(st, axis=1) / 1e3
         stages = {name: {"median_us": float(np.median(dur[:, i])), "max_us": float(dur[:, i].max())}
                   for i, name in enumerate(names)}
-        stages["window_total_us"] = {"median_us": float(np.median(st[:, 6] - st[:, 0]) / 1e3),
-                                     "max_us": float((st[:, 6] - st[:, 0]).max() / 1e3)}
+        stages["window_total_us"] = {"median_us": float(np.median(st[:, 7] - st[:, 0]) / 1e3),
+                                     "max_us": float((st[:, 7] - st[:, 0]).max() / 1e3)}
         n_med = float(np.median(np.diff(offsets)))
         stages["prim_ns_per_iteration"] = float(np.median(dur[:, 1]) * 1e3 / max(n_med - 1, 1))
 

@@ -105,6 +105,194 @@ __device__ __forceinline__ void load_coords(Real (&xr)[DPS], int j, bool xs, con
     }
 }
 
+// Coordinates of the current vertex, 16 bytes at a time.
+template <typename Real, int VEC>
+__device__ __forceinline__ void load_vec(Real (&c)[VEC], const Real* s_x, const Real* Xw, int cur, int k0, int DPS,
+                                         bool xs, int D) {
+    if (xs) {
+        if constexpr (sizeof(Real) == 4) {
+            const float4 q = *reinterpret_cast<const float4*>(s_x + cur * DPS + k0);
+            c[0] = q.x; c[1 % VEC] = q.y; c[2 % VEC] = q.z; c[3 % VEC] = q.w;
+        } else {
+            const double2 q = *reinterpret_cast<const double2*>(s_x + cur * DPS + k0);
+            c[0] = q.x; c[1 % VEC] = q.y;
+        }
+    } else {
+#pragma unroll
+        for (int kk = 0; kk < VEC; ++kk) c[kk] = (k0 + kk < D) ? Xw[(int64_t)cur * D + k0 + kk] : Real(0);
+    }
+}
+
+// Prim over one window by the active Prim warps (reference _kernels.py:164-320).
+// Writes edge `it` = (source, vertex, weight) into arena s0/s1/r0.  Returns
+// overflow flags (1 = a distance overflowed, 2 = internal inconsistency).
+template <typename Real, int PT, int SV, int DP, bool UNIT, typename Key>
+__device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<Real>& arena, const Real* s_x,
+                                           const Real* s_core, const Real* Xw, const Real* Dw, int n, bool xs,
+                                           Key (*s_key)[PT / 32], uint32_t (*s_idx)[PT / 32], int* s_scan) {
+    using T = RealTraits<Real>;
+    constexpr int PW = PT / 32;
+    constexpr int VEC = 16 / (int)sizeof(Real);
+    constexpr int DPS = DP > 0 ? DP : VEC;
+    constexpr Key SENTINEL = (Key)~(Key)0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int D = args.D;
+
+    // Per-slot state.  Slot s = tid*SV + v; xr holds the coordinates, act marks
+    // slots holding a vertex outside the tree.  (Packed f32x2 arithmetic is not
+    // used: ptxas contracts its multiply-add chains into FMA, which changes the
+    // rounding of the distance sums.)
+    Real xr[SV][DPS];
+    Real best[SV], thr[SV], core_r[SV];
+    int src[SV], vid[SV];
+    bool act[SV];
+    auto load_slot = [&](int v, int j) {
+        load_coords<Real, DP, DPS, VEC>(xr[v], j, xs, s_x, Xw, D);
+        if (!UNIT) core_r[v] = j >= 0 ? s_core[j] : Real(0);
+    };
+#pragma unroll
+    for (int v = 0; v < SV; ++v) {
+        const int j = tid * SV + v;
+        vid[v] = j < n ? j : -1;
+        act[v] = j < n && j != 0;  // vertex 0 starts the tree (_kernels.py:210-213)
+        best[v] = T::inf();
+        thr[v] = T::inf();
+        src[v] = 1;  // reference initial source (_kernels.py:167)
+        core_r[v] = Real(0);
+        load_slot(v, vid[v]);
+    }
+
+    int cur = 0;
+    int overflow = 0;
+    Real acc_max = Real(0);
+    int live = n;
+    int aw = (n + 32 * SV - 1) / (32 * SV);
+    if (aw > PW) aw = PW;
+    if (warp >= aw) return 0;
+    for (int it = 0; it < n - 1; ++it) {
+        const int remaining = n - 1 - it;  // vertices still outside the tree
+        if (live - remaining >= 32 * SV) {
+            // ---- compaction over the active warps ----------------------------
+            int count = 0;
+#pragma unroll
+            for (int v = 0; v < SV; ++v) count += act[v] ? 1 : 0;
+            int total = 0;
+            int pos = active_exclusive_scan(count, aw, s_scan, total);
+            int16_t* stage_j = arena.s2;
+            int16_t* stage_src = arena.s3;
+            Real* stage_best = arena.r1;
+#pragma unroll
+            for (int v = 0; v < SV; ++v) {
+                if (act[v]) {
+                    stage_j[pos] = (int16_t)vid[v];
+                    stage_src[pos] = (int16_t)src[v];
+                    stage_best[pos] = best[v];
+                    ++pos;
+                }
+            }
+            bar_sync(kBarIter, aw * 32);
+            live = total;
+#pragma unroll
+            for (int v = 0; v < SV; ++v) {
+                const int slot = tid * SV + v;
+                if (slot < live) {
+                    vid[v] = stage_j[slot];
+                    src[v] = stage_src[slot];
+                    best[v] = stage_best[slot];
+                    thr[v] = T::mul_ru(best[v], best[v]);
+                    act[v] = true;
+                } else {
+                    vid[v] = -1;
+                    act[v] = false;
+                }
+                load_slot(v, vid[v]);
+            }
+            bar_sync(kBarIter, aw * 32);  // staging slots may be rewritten afterwards
+            const int naw = (live + 32 * SV - 1) / (32 * SV);
+            aw = naw < 1 ? 1 : naw;
+            if (warp >= aw) break;  // this warp has no slots left (warp-uniform)
+        }
+        const Real core_cur = UNIT ? Real(0) : s_core[cur];
+        Real acc[SV];
+        if constexpr (DP > 0) {
+#pragma unroll
+            for (int v = 0; v < SV; ++v) acc[v] = Real(0);
+#pragma unroll
+            for (int k0 = 0; k0 < DPS; k0 += VEC) {
+                Real c[VEC];
+                load_vec<Real, VEC>(c, s_x, Xw, cur, k0, DPS, xs, D);
+#pragma unroll
+                for (int v = 0; v < SV; ++v)
+#pragma unroll
+                    for (int kk = 0; kk < VEC; ++kk) {
+                        const Real delta = T::sub(c[kk], xr[v][k0 + kk]);
+                        acc[v] = T::add(acc[v], T::mul(delta, delta));
+                    }
+            }
+        } else {
+            // Matrix variant: row `cur` of the window's distance block.
+            const Real* __restrict__ row = Dw + (int64_t)cur * (int64_t)((n + 3) & ~3);
+#pragma unroll
+            for (int v = 0; v < SV; ++v) acc[v] = act[v] ? __ldcg(row + vid[v]) : Real(0);
+        }
+        Key lkey = SENTINEL;
+        uint32_t lidx = 0xffffffffu;
+#pragma unroll
+        for (int v = 0; v < SV; ++v) {
+            if constexpr (DP > 0) {
+                // sqrt_rn is monotone and best representable: acc >= RU(best^2)
+                // gives sqrt_rn(acc) >= best, so no strict improvement.
+                acc_max = act[v] ? T::maxr(acc_max, acc[v]) : acc_max;
+                const Real cm = UNIT ? Real(0) : T::maxr(core_cur, core_r[v]);
+                if (act[v] && acc[v] < thr[v] && (UNIT || cm < best[v])) {
+                    const Real d = T::sqrt_rn(acc[v]);
+                    const Real wgt = UNIT ? d : T::maxr(cm, d);
+                    if (wgt < best[v]) {  // strict: equal weights keep the older source
+                        best[v] = wgt;
+                        src[v] = cur;
+                        thr[v] = T::mul_ru(wgt, wgt);
+                    }
+                }
+            } else {
+                if (act[v]) {
+                    const Real d = acc[v];
+                    overflow |= !(d <= T::kMax);
+                    const Real wgt = UNIT ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
+                    if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
+                }
+            }
+            const Key key = act[v] ? T::key(best[v]) : SENTINEL;
+            const uint32_t j = (uint32_t)vid[v];
+            if (key < lkey || (key == lkey && j < lidx)) { lkey = key; lidx = j; }
+        }
+        warp_argmin(lkey, lidx);
+        const int buf = it & 1;
+        if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
+        bar_sync(kBarIter, aw * 32);
+        Key gk = lane < aw ? s_key[buf][lane] : SENTINEL;
+        uint32_t gi = lane < aw ? s_idx[buf][lane] : 0xffffffffu;
+        warp_argmin(gk, gi);
+        const int next = (int)gi;
+        // The owner of the winner records the edge; its slot leaves the tree set.
+#pragma unroll
+        for (int v = 0; v < SV; ++v) {
+            if (vid[v] == next && act[v]) {
+                arena.s0[it] = (int16_t)src[v];
+                arena.s1[it] = (int16_t)next;
+                arena.r0[it] = best[v];
+                act[v] = false;
+            }
+        }
+        if (next < 0 || next >= n) {  // unreachable: a non-tree vertex always remains
+            overflow |= 2;
+            break;
+        }
+        cur = next;
+    }
+    if (DP > 0) overflow |= !(acc_max <= T::kMax);
+    return overflow;
+}
+
 struct WindowMeta {
     int w;      // window index, -1 = queue exhausted
     int n;
@@ -114,7 +302,7 @@ struct WindowMeta {
 // Dynamic shared memory: n_arenas arenas of arena_stride bytes, then the
 // staged window (x_off) and its core distances (core_off); see the plan layer.
 template <typename Real, int PT, int SV, int DP>
-__global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs args) {
+__global__ void __launch_bounds__(PT + 32, 1) hdb_forward_kernel(const ForwardArgs args) {
     using T = RealTraits<Real>;
     using Key = typename T::Bits;
     constexpr int PW = PT / 32;
@@ -150,6 +338,7 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
             if (meta.w < 0) return;
             if (!meta.skip) {
                 const int w = meta.w, n = meta.n, m = n - 1;
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 3] = global_ns();
                 const int64_t base = args.offsets[w];
                 const int64_t ebase = base - w;
                 Arena<Real> a = Arena<Real>::carve(smem + (size_t)b * args.arena_stride, n);
@@ -161,7 +350,7 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
                     }
                 }
                 sort_edges_warp<Real>(a, m);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 3] = global_ns();
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
                 if (args.order)
                     for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
                 __syncwarp();
@@ -173,7 +362,7 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
                 }
                 __syncwarp();
                 linkage_warp<Real>(a, n);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 5] = global_ns();
                 if (args.link_lr) {
                     for (int i = lane; i < m; i += 32) {
                         args.link_lr[2 * (ebase + i)] = a.s4[i];
@@ -184,7 +373,7 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
                 }
                 __syncwarp();
                 const int next_label = condense_warp<Real>(a, n, args.mcs);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 5] = global_ns();
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
                 if (args.cl_parent) {
                     for (int c = lane; c < next_label - n; c += 32) {
                         args.cl_parent[base + c] = a.s2[c];
@@ -201,7 +390,7 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
                     for (int i = lane; i < n; i += 32) args.point_parent[base + i] = a.s9[i];
                     if (lane == 0) args.n_clusters[w] = next_label - n;
                 }
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
+                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 7] = global_ns();
             }
             __syncwarp();
             __threadfence_block();
@@ -262,168 +451,11 @@ __global__ void __launch_bounds__(PT + 32) hdb_forward_kernel(const ForwardArgs 
 
         int overflow = 0;
         if (!invalid) {
-            Real xr[SV][DPS];
-            Real best[SV];
-            Real thr[SV];  // RU(best^2)
-            Real core_r[SV];
-            int src[SV];
-            int vid[SV];
-            uint32_t in_tree = 0;
-#pragma unroll
-            for (int v = 0; v < SV; ++v) {
-                const int j = tid * SV + v;
-                vid[v] = j < n ? j : -1;
-                best[v] = T::inf();
-                thr[v] = T::inf();
-                src[v] = 1;  // reference initial source (_kernels.py:167)
-                core_r[v] = Real(0);
-                load_coords<Real, DP, DPS, VEC>(xr[v], vid[v], xs, s_x, Xw, D);
-                if (!args.unit_core && j < n) core_r[v] = s_core[j];
-            }
-            if (tid == 0) in_tree = 1u;  // vertex 0 starts the tree (_kernels.py:210-213)
             if (args.stage_ns && tid == 0) args.stage_ns[8 * w + 1] = global_ns();
-
-            int cur = 0;
-            Real acc_max = Real(0);
-            int live = n;
-            int aw = (n + 32 * SV - 1) / (32 * SV);  // active warps
-            if (aw > PW) aw = PW;
-            if (warp < aw) {
-                for (int it = 0; it < n - 1; ++it) {
-                    const int remaining = n - 1 - it;  // vertices still outside the tree
-                    if (live - remaining >= 32 * SV) {
-                        // ---- compaction over the active warps --------------
-                        int count = 0;
-#pragma unroll
-                        for (int v = 0; v < SV; ++v)
-                            count += (tid * SV + v < live && !((in_tree >> v) & 1u)) ? 1 : 0;
-                        int total = 0;
-                        int pos = active_exclusive_scan(count, aw, s_scan, total);
-                        int16_t* stage_j = arena.s2;
-                        int16_t* stage_src = arena.s3;
-                        Real* stage_best = arena.r1;
-#pragma unroll
-                        for (int v = 0; v < SV; ++v) {
-                            if (tid * SV + v < live && !((in_tree >> v) & 1u)) {
-                                stage_j[pos] = (int16_t)vid[v];
-                                stage_src[pos] = (int16_t)src[v];
-                                stage_best[pos] = best[v];
-                                ++pos;
-                            }
-                        }
-                        bar_sync(kBarIter, aw * 32);
-                        live = total;
-                        in_tree = 0;
-#pragma unroll
-                        for (int v = 0; v < SV; ++v) {
-                            const int slot = tid * SV + v;
-                            if (slot < live) {
-                                vid[v] = stage_j[slot];
-                                src[v] = stage_src[slot];
-                                best[v] = stage_best[slot];
-                                thr[v] = T::mul_ru(best[v], best[v]);
-                                if (!args.unit_core) core_r[v] = s_core[vid[v]];
-                                load_coords<Real, DP, DPS, VEC>(xr[v], vid[v], xs, s_x, Xw, D);
-                            } else {
-                                vid[v] = -1;
-                            }
-                        }
-                        bar_sync(kBarIter, aw * 32);  // staging slots may be rewritten afterwards
-                        const int naw = (live + 32 * SV - 1) / (32 * SV);
-                        aw = naw < 1 ? 1 : naw;
-                        if (warp >= aw) break;  // this warp has no slots left (warp-uniform)
-                    }
-                    const Real core_cur = args.unit_core ? Real(0) : s_core[cur];
-                    Real acc[SV];
-#pragma unroll
-                    for (int v = 0; v < SV; ++v) acc[v] = Real(0);
-                    if (DP > 0) {
-#pragma unroll
-                        for (int k0 = 0; k0 < DPS; k0 += VEC) {
-                            Real c[VEC];
-                            if (xs) {
-                                if constexpr (sizeof(Real) == 4) {
-                                    const float4 q = *reinterpret_cast<const float4*>(s_x + cur * DPS + k0);
-                                    c[0] = q.x; c[1] = q.y; c[2 % VEC] = q.z; c[3 % VEC] = q.w;
-                                } else {
-                                    const double2 q = *reinterpret_cast<const double2*>(s_x + cur * DPS + k0);
-                                    c[0] = q.x; c[1 % VEC] = q.y;
-                                }
-                            } else {
-#pragma unroll
-                                for (int kk = 0; kk < VEC; ++kk)
-                                    c[kk] = (k0 + kk < D) ? Xw[(int64_t)cur * D + k0 + kk] : Real(0);
-                            }
-#pragma unroll
-                            for (int v = 0; v < SV; ++v) {
-#pragma unroll
-                                for (int kk = 0; kk < VEC; ++kk) {
-                                    const Real delta = T::sub(c[kk], xr[v][(k0 + kk) % DPS]);
-                                    acc[v] = T::add(acc[v], T::mul(delta, delta));
-                                }
-                            }
-                        }
-                    } else {
-                        // Matrix variant: row `cur` of the window's distance block.
-                        const Real* __restrict__ row = Dw + (int64_t)cur * (int64_t)((n + 3) & ~3);
-#pragma unroll
-                        for (int v = 0; v < SV; ++v)
-                            if (tid * SV + v < live && !((in_tree >> v) & 1u)) acc[v] = __ldcg(row + vid[v]);
-                    }
-                    Key lkey = SENTINEL;
-                    uint32_t lidx = 0xffffffffu;
-#pragma unroll
-                    for (int v = 0; v < SV; ++v) {
-                        if (tid * SV + v < live && !((in_tree >> v) & 1u)) {
-                            if (DP > 0) {
-                                acc_max = T::maxr(acc_max, acc[v]);
-                                const Real cm = args.unit_core ? Real(0) : T::maxr(core_cur, core_r[v]);
-                                if (cm < best[v] && acc[v] < thr[v]) {
-                                    const Real d = T::sqrt_rn(acc[v]);
-                                    const Real wgt = T::maxr(cm, d);
-                                    if (wgt < best[v]) {
-                                        best[v] = wgt;
-                                        src[v] = cur;
-                                        thr[v] = T::mul_ru(wgt, wgt);
-                                    }
-                                }
-                            } else {
-                                const Real d = acc[v];
-                                overflow |= !(d <= T::kMax);
-                                const Real wgt = args.unit_core ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
-                                if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
-                            }
-                            const Key key = T::key(best[v]);
-                            const uint32_t j = (uint32_t)vid[v];
-                            if (key < lkey || (key == lkey && j < lidx)) { lkey = key; lidx = j; }
-                        }
-                    }
-                    warp_argmin(lkey, lidx);
-                    const int buf = it & 1;
-                    if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
-                    bar_sync(kBarIter, aw * 32);
-                    Key gk = lane < aw ? s_key[buf][lane] : SENTINEL;
-                    uint32_t gi = lane < aw ? s_idx[buf][lane] : 0xffffffffu;
-                    warp_argmin(gk, gi);
-                    const int next = (int)gi;
-                    // Owner of the winner records the edge and joins the tree.
-#pragma unroll
-                    for (int v = 0; v < SV; ++v) {
-                        if (vid[v] == next && tid * SV + v < live) {
-                            arena.s0[it] = (int16_t)src[v];
-                            arena.s1[it] = (int16_t)next;
-                            arena.r0[it] = best[v];
-                            in_tree |= 1u << v;
-                        }
-                    }
-                    if (next < 0 || next >= n) {  // unreachable: a non-tree vertex always remains
-                        overflow |= 2;
-                        break;
-                    }
-                    cur = next;
-                }
-            }
-            if (DP > 0) overflow |= !(acc_max <= T::kMax);
+            if (args.unit_core)
+                overflow = prim_window<Real, PT, SV, DP, true>(args, arena, s_x, s_core, Xw, Dw, n, xs, s_key, s_idx, s_scan);
+            else
+                overflow = prim_window<Real, PT, SV, DP, false>(args, arena, s_x, s_core, Xw, Dw, n, xs, s_key, s_idx, s_scan);
         }
         if (overflow) atomicOr(&s_flags[par], overflow << 1);
         bar_sync(kBarStart, PT);

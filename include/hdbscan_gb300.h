@@ -79,7 +79,7 @@ typedef struct hdb_exports {
     void* core;            /* [T]   core distances (Real); written when min_samples > 2 */
     int32_t* core_nbr;     /* [T]   ms-th nearest neighbour in (distance, index) order */
     int64_t* stage_ns;     /* [B,8] device timestamps (ns) per window: start, Prim start, Prim end,
-                                    sort end, linkage end, condensation end, selection end */
+                                    hierarchy start, sort end, linkage end, condensation end, labels end */
 } hdb_exports_t;
 
 /* Library version (HDB_VERSION). */
