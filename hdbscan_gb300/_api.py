@@ -81,7 +81,7 @@ def validate_limits(n, min_cluster_size, min_samples, cluster_selection_epsilon,
         raise ValueError("min_samples must not exceed the number of samples")
     if min_cluster_size > np.iinfo(np.int32).max:
         raise ValueError("min_cluster_size must fit in int32")
-    if cluster_selection_epsilon > np.finfo(precision).max:
+    if float(cluster_selection_epsilon) > float(np.finfo(precision).max):
         raise ValueError("cluster_selection_epsilon is not representable in the requested precision")
 
 

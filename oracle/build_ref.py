@@ -56,9 +56,18 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> bool:
                      "const Real* options, int* labels, int* integers, Real* reals) {\n")
         parts.append(kernels.CLUSTER_SOURCE)
         parts.append("\n}\n")
+        # Linkage-only prefix (Prim + sort + union-find), as the reference's own
+        # kernel tests build it: the full body reuses left/right/sizes later.
+        parts.append("static void linkage_one(int hdb_gid, const Real* distances, const Real* core, const int* params, "
+                     "const Real* options, int* labels, int* integers, Real* reals) {\n")
+        parts.append(kernels.CLUSTER_SOURCE.split(kernels.CONDENSE_SOURCE)[0])
+        parts.append("\n}\n")
         parts.append(f'#define HDB_REF_SUFFIX {suffix}\n#include "../ref_driver.inc"\n#undef HDB_REF_SUFFIX\n')
         parts.append("#undef REAL_MAX\n}\n")
-    (OUT / "ref_kernels.cpp").write_text("".join(parts))
+    text = "".join(parts)
+    target = OUT / "ref_kernels.cpp"
+    if not target.exists() or target.read_text() != text:  # keep the mtime when nothing changed
+        target.write_text(text)
     layout = {
         "INTEGER_ARRAYS": list(kernels.INTEGER_ARRAYS),
         "REAL_ARRAYS": list(kernels.REAL_ARRAYS),
