@@ -41,6 +41,9 @@ def _declare(handle):
     sig = {
         "hdb_version": (ctypes.c_int, []),
         "hdb_last_error": (ctypes.c_char_p, []),
+        "hdb_set_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
+        "hdb_get_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
+        "hdb_list_variants": (ctypes.c_int, [ctypes.c_int, _P, ctypes.c_int]),
         "hdb_plan_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint]),
         "hdb_plan_destroy": (ctypes.c_int, [_P]),
@@ -66,7 +69,8 @@ def _declare(handle):
 
 
 # Every symbol include/hdbscan_gb300.h declares.
-SYMBOLS = ("hdb_version", "hdb_last_error", "hdb_plan_create", "hdb_plan_destroy", "hdb_plan_workspace_bytes",
+SYMBOLS = ("hdb_version", "hdb_last_error", "hdb_set_tuning", "hdb_get_tuning", "hdb_list_variants",
+           "hdb_plan_create", "hdb_plan_destroy", "hdb_plan_workspace_bytes",
            "hdb_plan_describe", "hdb_plan_forward", "hdb_plan_capture", "hdb_plan_replay", "hdb_plan_backward",
            "hdb_cluster_workspace_bytes", "hdb_cluster_f32", "hdb_cluster_f64", "hdb_cluster_noalloc")
 
@@ -80,6 +84,9 @@ def lib():
             handle = ctypes.CDLL(str(path))
             _declare(handle)
             _lib = handle
+            from . import autotune
+
+            autotune.apply_table(handle)
     return _lib
 
 

@@ -113,9 +113,26 @@ int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
 
 cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise_dynamic_smem(func, bytes); }
 
-// Autotune table: (Prim threads, slots per thread) by window size, register
-// dimensions by D.  Windows whose coordinates do not fit the register budget
-// (64 32-bit registers of coordinates per thread) use the matrix variant.
+// Autotune rules: the first rule whose (precision, core mode, n, D) bounds
+// match a window picks its variant (Prim threads, slots per thread, register
+// dimensions; dims 0 = matrix variant).  The compiled-in defaults below are
+// replaced at run time by hdb_set_tuning (the package loads the table that
+// hdbscan_gb300/autotune.py measured).  A rule naming a variant that is not
+// compiled falls through to the next rule, and the shape heuristic backs up
+// the whole table.
+struct TuningRule {
+    int precision;  // HDB_F32 / HDB_F64 / -1 any
+    int unit;       // 1 = min_samples <= 2, 0 = core distances, -1 any
+    int n_max;
+    int d_max;
+    int threads;
+    int slots;
+    int dims;       // register dimensions; 0 = matrix variant
+};
+
+std::mutex g_tuning_mutex;
+std::vector<TuningRule> g_tuning;  // empty = defaults
+
 void class_shape(int n, int* threads, int* v) {
     if (n <= 64) { *threads = 32; *v = 2; }
     else if (n <= 128) { *threads = 64; *v = 2; }
@@ -126,24 +143,39 @@ void class_shape(int n, int* threads, int* v) {
     else { *threads = 512; *v = 8; }
 }
 
-const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int precision, int n, int D,
-                                          bool force_matrix) {
-    int threads, v;
-    class_shape(n, &threads, &v);
-    int dp = 0;
-    if (!force_matrix) {
-        const int words = precision == HDB_F32 ? 1 : 2;  // registers per coordinate
-        for (int option : {8, 16, 32})
-            if (D <= option && v * option * words <= 64) { dp = option; break; }
-    }
-    const hdb::ForwardVariant* fallback = nullptr;
+const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int threads, int v, int dp) {
     for (int i = 0; i < k.n_forward; ++i) {
         const hdb::ForwardVariant& f = k.forward[i];
-        if (f.threads != threads || f.v != v) continue;
-        if (f.dp == dp) return &f;
-        if (f.dp == 0) fallback = &f;
+        if (f.threads == threads && f.v == v && f.dp == dp) return &f;
     }
-    return fallback;
+    return nullptr;
+}
+
+const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int precision, int n, int D,
+                                          bool unit, bool force_matrix) {
+    int threads, v;
+    class_shape(n, &threads, &v);
+    if (force_matrix) return find_variant(k, threads, v, 0);
+    {
+        std::lock_guard<std::mutex> lock(g_tuning_mutex);
+        for (const TuningRule& r : g_tuning) {
+            if ((r.precision >= 0 && r.precision != precision) || (r.unit >= 0 && r.unit != (unit ? 1 : 0)) ||
+                n > r.n_max || D > r.d_max || r.threads * r.slots < n || (r.dims > 0 && D > r.dims))
+                continue;
+            const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims);
+            if (f) return f;
+        }
+    }
+    // Defaults.  float64 SIMT is a small fraction of float32 on GB300, so
+    // float64 windows use the matrix variant: the distance block is computed
+    // once per pair by a grid spread over every SM, and Prim only reads rows.
+    int dp = 0;
+    if (precision == HDB_F32) {
+        for (int option : {8, 16, 32})
+            if (D <= option && v * option <= 64) { dp = option; break; }
+    }
+    const hdb::ForwardVariant* f = find_variant(k, threads, v, dp);
+    return f ? f : find_variant(k, threads, v, 0);
 }
 
 // Dynamic shared memory available to a forward variant next to its static use.
@@ -198,7 +230,7 @@ int build_plan(hdb_plan* p) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return size_of(a) > size_of(b); });
     for (int w : order) {
         const int n = size_of(w);
-        const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, force_matrix);
+        const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, unit, force_matrix);
         if (!fv) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(n) + " points");
         size_t budget = 0;
         int rc = smem_budget(fv->func, optin, &budget);
@@ -520,6 +552,44 @@ int cluster_dense(int precision, const void* X, int batch, int n, int dims, int 
 extern "C" {
 
 int hdb_version(void) { return HDB_VERSION; }
+
+int hdb_set_tuning(const int32_t* rules, int n_rules) {
+    if (n_rules < 0 || (n_rules > 0 && !rules)) return fail(HDB_E_INVALID, "tuning rules must be a [n, 7] int32 array");
+    std::vector<TuningRule> table;
+    for (int i = 0; i < n_rules; ++i) {
+        const int32_t* r = rules + 7 * i;
+        TuningRule t{r[0], r[1], r[2], r[3], r[4], r[5], r[6]};
+        if (t.precision < -1 || t.precision > 1 || t.unit < -1 || t.unit > 1 || t.n_max < 2 || t.d_max < 1 ||
+            t.threads < 32 || t.threads % 32 || t.threads > 992 || t.slots < 1 || t.dims < 0)
+            return fail(HDB_E_INVALID, "tuning rule " + std::to_string(i) + " is out of range");
+        table.push_back(t);
+    }
+    std::lock_guard<std::mutex> lock(g_tuning_mutex);
+    g_tuning = std::move(table);
+    return HDB_OK;
+}
+
+int hdb_list_variants(int precision, int32_t* out, int capacity) {
+    if (precision != HDB_F32 && precision != HDB_F64) return fail(HDB_E_INVALID, "precision must be 'float32' or 'float64'");
+    const hdb::PrecisionKernels& k = precision == HDB_F32 ? hdb::kernels_f32() : hdb::kernels_f64();
+    for (int i = 0; i < k.n_forward && i < capacity && out; ++i) {
+        out[3 * i] = k.forward[i].threads;
+        out[3 * i + 1] = k.forward[i].v;
+        out[3 * i + 2] = k.forward[i].dp;
+    }
+    return k.n_forward;
+}
+
+int hdb_get_tuning(int32_t* rules, int capacity) {
+    std::lock_guard<std::mutex> lock(g_tuning_mutex);
+    const int count = (int)g_tuning.size();
+    for (int i = 0; i < count && i < capacity && rules; ++i) {
+        const TuningRule& t = g_tuning[i];
+        const int32_t v[7] = {t.precision, t.unit, t.n_max, t.d_max, t.threads, t.slots, t.dims};
+        for (int j = 0; j < 7; ++j) rules[7 * i + j] = v[j];
+    }
+    return count;
+}
 
 const char* hdb_last_error(void) { return g_error.c_str(); }
 

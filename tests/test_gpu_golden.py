@@ -22,7 +22,7 @@ def _groups(family):
     groups = defaultdict(list)
     for name, case in golden.load(family).items():
         mcs, ms, eps = case["params"]
-        groups[(int(mcs), int(ms), float(eps))].append((name, case))
+        groups[(int(mcs), int(ms), float(eps), case["x"].shape[1])].append((name, case))
     return groups
 
 
@@ -39,7 +39,7 @@ def test_golden_family(cuda, family, precision, force_matrix):
     from hdbscan_gb300._cuda import cluster_ragged, pack
 
     checked = 0
-    for (mcs, ms, eps), items in _groups(family).items():
+    for (mcs, ms, eps, _dims), items in _groups(family).items():
         items = [(n, c) for n, c in items if int(np.ravel(c[f"{precision}/ref_status"])[0]) == 0]
         if not items:
             continue
