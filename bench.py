@@ -180,7 +180,11 @@ def main():
     parser.add_argument("--cpu-windows", type=int, default=256)
     parser.add_argument("--plain-passes", type=int, default=2)
     parser.add_argument("--skip-cpu", action="store_true")
+    parser.add_argument("--windows", type=int, default=None,
+                        help="override the config's window count (small cases for ncu captures)")
     parser.add_argument("--stages", action="store_true", help="report per-stage device time of the forward kernel")
+    parser.add_argument("--backward", choices=("auto", "on", "off"), default="auto",
+                        help="time forward+backward (default: on for the c4/c5 differentiation configs)")
     parser.add_argument("--profile", action="store_true",
                         help="only warm-up + timed graph replays (for ncu captures); prints nothing else")
     args = parser.parse_args()
@@ -191,7 +195,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from hdbscan_gb300 import synthetic
 
-    packed64, offsets, params = synthetic.make(args.config)
+    packed64, offsets, params = synthetic.make(args.config, **({"windows": args.windows} if args.windows else {}))
     if args.impl == "reference":
         if rank == 0:
             run_reference_arm(args, packed64, offsets, params)
@@ -223,13 +227,25 @@ def main():
     plan = Plan(offsets, D, min_cluster_size=mcs, min_samples=ms, cluster_selection_epsilon=eps,
                 precision=precision)
     workspace = plan.workspace()
-    labels, status = plan.capture(X, workspace=workspace)
+    backward = args.backward == "on" or (args.backward == "auto" and args.config in ("c4", "c5"))
+    exports = plan.export_buffers(hierarchy=False, gradients=True) if backward else None
+    labels, status = plan.capture(X, workspace=workspace, exports=exports)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
     stream = torch.cuda.current_stream(device)
+    if backward:
+        # Loss L = sum_i w_i * merge_weight_i with w ~ N(0, 1) seeded.
+        grad_w = torch.as_tensor(np.random.default_rng(7).normal(size=plan.edges), dtype=dtype, device=device)
+        dX = torch.zeros_like(X)
+
+    def step():
+        plan.replay()
+        if backward:
+            dX.zero_()
+            plan.backward(X, exports, grad_w, dX=dX, workspace=workspace)
 
     # Warm-up + correctness of the graph run.
     for _ in range(args.warmup):
-        plan.replay()
+        step()
     torch.cuda.synchronize()
     raise_for_status(int(status.item()))
     graph_labels = labels.cpu().numpy().copy()
@@ -244,7 +260,7 @@ def main():
             flush.fill_(1)
             start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             start.record(stream)
-            plan.replay()
+            step()
             end.record(stream)
             end.synchronize()
             step_ms.append(start.elapsed_time(end))
@@ -299,11 +315,18 @@ def main():
             one_ws[n] = plain_plans[n].workspace()
     plain_status = torch.empty(1, dtype=torch.int32, device=device)
 
+    plain_exports = {n: plain_plans[n].export_buffers(hierarchy=False, gradients=True) for n in plain_plans} \
+        if backward else {}
+
     def plain_pass():
         for w in range(B):
             lo, hi = int(offsets[w]), int(offsets[w + 1])
             p = plain_plans[hi - lo]
-            p.forward(X[lo:hi], labels=plain_labels[lo:hi], workspace=one_ws[hi - lo], status=plain_status)
+            ex = plain_exports.get(hi - lo)
+            p.forward(X[lo:hi], labels=plain_labels[lo:hi], workspace=one_ws[hi - lo], status=plain_status,
+                      exports=ex)
+            if backward:
+                p.backward(X[lo:hi], ex, grad_w[lo - w:hi - w - 1], dX=dX[lo:hi], workspace=one_ws[hi - lo])
 
     plain_pass()
     torch.cuda.synchronize()
@@ -326,7 +349,14 @@ def main():
     for step in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        if uniform:
+        if backward:
+            Xd = pinned.to(device, non_blocking=True).requires_grad_(True)
+            weights, result = hdbscan_gb300.merge_weights(Xd, offsets, min_cluster_size=mcs, min_samples=ms,
+                                                          cluster_selection_epsilon=eps, precision=precision)
+            loss = (weights * grad_w).sum()
+            loss.backward()
+            loss_value = float(loss.item())
+        elif uniform:
             n = int(offsets[1])
             result = hdbscan_gb300.hdbscan(pinned.view(B, n, D).to(device, non_blocking=True),
                                            min_cluster_size=mcs, min_samples=ms,
@@ -378,6 +408,8 @@ def main():
     if traffic_path.exists():
         traffic = json.loads(traffic_path.read_text()).get("dram_bytes_per_launch")
     launches_per_step = len(describe["classes"]) + len(describe["core"]) + (1 if describe["distance_tiles"] else 0)
+    if backward:
+        launches_per_step += 2  # dX zeroing + backward kernel
     line = {
         "metric": "windows_per_s", "value": value, "unit": "windows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -389,7 +421,8 @@ def main():
         "speedup_vs_plain": value / plain_value,
         "labels_bit_exact": {"graph_vs_oracle_sample": oracle_exact, "e2e_vs_graph": e2e_exact},
         "e2e": {"value": e2e_value, "unit": "windows/s", "h2d_bytes_per_step": int(host.nbytes),
-                "d2h_bytes_per_step": int(T * 4 + 4)},
+                "d2h_bytes_per_step": int(T * 4 + (host.itemsize if backward else 4))},
+        "mode": "forward+backward" if backward else "forward",
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
