@@ -20,7 +20,8 @@ CSRC = PACKAGE / "csrc"
 BUILD = PACKAGE / "_build"
 LIBRARY = PACKAGE / "libhdbscan_gb300.so"
 INCLUDE = PACKAGE.parent / "include"
-SOURCES = ("hdb_capi.cu", "hdb_kernels_f32.cu", "hdb_kernels_f64.cu", "hdb_noalloc.cu")
+SOURCES = ("hdb_capi.cu", "hdb_kernels_f32.cu", "hdb_kernels_f64.cu", "hdb_cluster_f32.cu", "hdb_cluster_f64.cu",
+           "hdb_noalloc.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 FLAGS = ("-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 

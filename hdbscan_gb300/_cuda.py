@@ -50,7 +50,7 @@ class Plan:
     """
 
     def __init__(self, offsets, dims, *, min_cluster_size=5, min_samples=None, cluster_selection_epsilon=0.0,
-                 precision="float32", force_matrix=False, device=None):
+                 precision="float32", force_matrix=False, one_persistent=False, device=None):
         if precision not in _DTYPES:
             raise ValueError("precision must be 'float32' or 'float64'")
         _require_gpu()
@@ -68,7 +68,8 @@ class Plan:
         self.epsilon = float(cluster_selection_epsilon)
         self.precision = precision
         self.torch_dtype, self.numpy_dtype, code = _DTYPES[precision]
-        self.flags = _lib.HDB_FLAG_FORCE_MATRIX if force_matrix else 0
+        self.flags = (_lib.HDB_FLAG_FORCE_MATRIX if force_matrix else 0) | (
+            _lib.HDB_FLAG_ONE_PERSISTENT if one_persistent else 0)
         lib = _lib.lib()
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):

@@ -15,6 +15,7 @@ HDB_F32 = 0
 HDB_F64 = 1
 HDB_FLAG_FORCE_MATRIX = 1
 HDB_FLAG_NO_GRAPH_STREAMS = 2
+HDB_FLAG_ONE_PERSISTENT = 4
 STATUS_OVERFLOW = 1
 STATUS_NONFINITE = 2
 STATUS_INTERNAL = 4

@@ -4,12 +4,17 @@ For every (precision, core mode, n bucket, D bucket) the tuner builds a batch
 of seeded Gaussian-mixture windows of the bucket's largest size, large enough
 to fill every SM, times each compiled variant that can hold such a window
 (`hdb_list_variants`: Prim threads x slots per thread, register dimensions or
-the materialized-matrix variant) and keeps the fastest.  The result is
+the materialized-matrix variant, CTAs per window) and keeps the fastest.  The result is
 written to autotune_table.json next to this file; the package applies it
 through `hdb_set_tuning` when the library loads.  Replaces the fixed launch
 choice of the reference (hdbscan_gpu/_cuda.py:82-88).
 
 Run on the target GPU:  python -m hdbscan_gb300.autotune [--quick]
+                        [--n 2048 4096] [--precision float32] (re-tune those
+                        buckets only; the other rules of the table are kept)
+
+The environment variable HDB_AUTOTUNE_TABLE names another table file to load,
+or "none" to run on the compiled-in defaults.
 """
 
 from __future__ import annotations
@@ -17,6 +22,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import os
 import time
 from pathlib import Path
 
@@ -27,14 +33,27 @@ N_BUCKETS = (64, 128, 256, 512, 1024, 2048, 4096)
 D_BUCKETS = (8, 16, 32, 64, 128)
 
 
+FIELDS = 8
+
+
 def _rules_array(rules):
-    flat = np.ascontiguousarray(np.asarray(rules, dtype=np.int32).reshape(-1, 7))
-    return flat
+    # Tables written before the cluster field existed hold 7-field rules: one CTA.
+    rows = [list(r) + [1] * (FIELDS - len(r)) for r in rules]
+    return np.ascontiguousarray(np.asarray(rows, dtype=np.int32).reshape(-1, FIELDS))
 
 
-def apply_table(lib, path: Path = TABLE) -> int:
-    """Load the committed table into the library; returns the number of rules."""
-    if not path.exists():
+def table_path() -> Path | None:
+    """The table the package loads: HDB_AUTOTUNE_TABLE, else the committed one; None = defaults."""
+    override = os.environ.get("HDB_AUTOTUNE_TABLE")
+    if override is None:
+        return TABLE
+    return None if override.lower() == "none" else Path(override)
+
+
+def apply_table(lib, path: Path | None = None) -> int:
+    """Load the tuning table into the library; returns the number of rules."""
+    path = table_path() if path is None else path
+    if path is None or not path.exists():
         return 0
     rules = [r["rule"] for r in json.loads(path.read_text())["rules"]]
     arr = _rules_array(rules)
@@ -46,9 +65,9 @@ def apply_table(lib, path: Path = TABLE) -> int:
 
 def variants(lib, precision_code):
     count = lib.hdb_list_variants(precision_code, None, 0)
-    out = np.zeros(3 * count, np.int32)
+    out = np.zeros(4 * count, np.int32)
     lib.hdb_list_variants(precision_code, out.ctypes.data_as(ctypes.c_void_p), count)
-    return [tuple(int(v) for v in out[3 * i:3 * i + 3]) for i in range(count)]
+    return [tuple(int(v) for v in out[4 * i:4 * i + 4]) for i in range(count)]
 
 
 def _windows(rng, batch, n, dims):
@@ -78,7 +97,7 @@ def _time_plan(plan, X, repeats):
     return float(np.median(times)), labels
 
 
-def tune(quick=False, out: Path = TABLE, log=print):
+def tune(quick=False, out: Path = TABLE, log=print, sizes=None, precisions=None):
     import torch
 
     from . import _lib
@@ -89,12 +108,15 @@ def tune(quick=False, out: Path = TABLE, log=print):
     rng = np.random.default_rng(20261203)
     records = []
     for precision, code in (("float32", _lib.HDB_F32), ("float64", _lib.HDB_F64)):
+        if precisions and precision not in precisions:
+            continue
         available = variants(lib, code)
         for unit in (1, 0):
             ms = 2 if unit else 8
-            for n in (N_BUCKETS[2:5:2] if quick else N_BUCKETS):
+            for n in (sizes or (N_BUCKETS[2:5:2] if quick else N_BUCKETS)):
                 for dims in (D_BUCKETS[1:3] if quick else D_BUCKETS):
-                    cands = [v for v in available if v[0] * v[1] >= n and (v[2] == 0 or dims <= v[2])]
+                    cands = [v for v in available if v[0] * v[1] * v[3] >= n and (v[2] == 0 or dims <= v[2])
+                             and (v[3] == 1 or n > 1024)]
                     # The smallest slot shape that holds n, plus every matrix variant.
                     if not cands:
                         continue
@@ -106,20 +128,21 @@ def tune(quick=False, out: Path = TABLE, log=print):
                         torch.float32 if precision == "float32" else torch.float64)
                     timings = []
                     reference_labels = None
-                    for threads, slots, dp in cands:
-                        rule = [code, unit, n, dims, threads, slots, dp]
+                    for threads, slots, dp, cluster in cands:
+                        rule = [code, unit, n, dims, threads, slots, dp, cluster]
                         arr = _rules_array([rule])
                         lib.hdb_set_tuning(arr.ctypes.data_as(ctypes.c_void_p), 1)
                         plan = Plan(offsets, dims, min_cluster_size=5, min_samples=ms, precision=precision)
                         desc = json.loads(plan.describe())["classes"][0]
-                        if (desc["threads"], desc["vertices_per_thread"], desc["register_dims"]) != (threads, slots, dp):
+                        if (desc["threads"], desc["vertices_per_thread"], desc["register_dims"],
+                                desc["cluster"]) != (threads, slots, dp, cluster):
                             continue  # the rule was not applicable (e.g. shared memory)
                         ms_time, labels = _time_plan(plan, X, 3 if quick else 5)
                         host = labels.cpu().numpy()
                         if reference_labels is None:
                             reference_labels = host
                         elif not np.array_equal(host, reference_labels):
-                            raise RuntimeError(f"variant {threads}x{slots}/{dp} changed the labels")
+                            raise RuntimeError(f"variant {threads}x{slots}/{dp}/c{cluster} changed the labels")
                         timings.append((ms_time, rule))
                         del plan
                     lib.hdb_set_tuning(None, 0)
@@ -130,11 +153,19 @@ def tune(quick=False, out: Path = TABLE, log=print):
                     records.append({"rule": best, "ms": best_ms, "windows": batch,
                                     "candidates": [{"rule": r, "ms": t} for t, r in timings]})
                     log(f"{precision} unit={unit} n<={n} D<={dims}: {best[4]}x{best[5]} dims={best[6]} "
-                        f"{best_ms:.3f} ms ({len(timings)} candidates)")
+                        f"cluster={best[7]} {best_ms:.3f} ms ({len(timings)} candidates)")
+    if sizes or precisions:
+        # Partial re-tune: keep the previous rules of every bucket not measured now.
+        measured = {tuple(r["rule"][:4]) for r in records}
+        if out.exists():
+            for old in json.loads(out.read_text())["rules"]:
+                old["rule"] = list(old["rule"]) + [1] * (FIELDS - len(old["rule"]))
+                if tuple(old["rule"][:4]) not in measured:
+                    records.append(old)
     # Most specific first: smaller n and D buckets are checked before larger ones.
     records.sort(key=lambda r: (r["rule"][0], -r["rule"][1], r["rule"][2], r["rule"][3]))
     table = {"device": torch.cuda.get_device_name(0), "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
-             "fields": ["precision", "unit_core", "n_max", "d_max", "threads", "slots", "dims"],
+             "fields": ["precision", "unit_core", "n_max", "d_max", "threads", "slots", "dims", "cluster"],
              "rules": records}
     out.write_text(json.dumps(table, indent=1) + "\n")
     apply_table(lib, out)
@@ -145,5 +176,7 @@ if __name__ == "__main__":
     parser = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     parser.add_argument("--quick", action="store_true")
     parser.add_argument("--out", type=Path, default=TABLE)
+    parser.add_argument("--n", type=int, nargs="*", help="only these n buckets")
+    parser.add_argument("--precision", nargs="*", choices=["float32", "float64"])
     args = parser.parse_args()
-    tune(args.quick, args.out)
+    tune(args.quick, args.out, sizes=args.n, precisions=args.precision)

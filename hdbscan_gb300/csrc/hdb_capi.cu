@@ -2,10 +2,16 @@
 //
 // A plan turns a ragged batch description into: per-window kernel variants
 // (the autotune table in choose_variant), window classes launched as
-// persistent grids over size-sorted queues on forked streams, the tile and
-// row work lists of the distance/core kernels, and one pinned host image of
-// every device table, uploaded by a single cudaMemcpyAsync per call so the
-// whole forward is capturable in a CUDA graph.
+// persistent grids over size-sorted queues, the tile and row work lists of
+// the distance/core kernels, and one pinned host image of every device table,
+// uploaded by a single cudaMemcpyAsync per call so the whole forward is
+// capturable in a CUDA graph.  The distance tiles and core distances run as
+// one chain on the caller's stream, class by class from the largest windows
+// down; each class's persistent forward is forked onto its own stream (higher
+// priority for larger windows) as soon as its own inputs are ready, so the
+// longest Prim loops start first and the remaining pre-work and smaller
+// classes fill the other SMs.  The order is explicit in the dependencies, so
+// a captured graph schedules exactly like the stream launch.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -37,6 +43,14 @@ int fail(int code, const std::string& message) {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+struct CoreLaunch {
+    const hdb::CoreVariant* cv = nullptr;  // null = select kernel
+    bool matrix = false;
+    std::vector<int32_t> items;             // (window, row) pairs
+    size_t items_off = 0;                   // byte offset in tables
+    size_t select_smem = 0;
+};
+
 struct WindowClass {
     const hdb::ForwardVariant* fv = nullptr;
     int x_in_smem = 0;
@@ -48,14 +62,10 @@ struct WindowClass {
     int grid = 0;
     size_t queue_off = 0;      // element offset into the queue table
     int ticket = 0;            // index into the ticket table
-};
-
-struct CoreLaunch {
-    const hdb::CoreVariant* cv = nullptr;  // null = select kernel
-    bool matrix = false;
-    std::vector<int32_t> items;             // (window, row) pairs
-    size_t items_off = 0;                   // byte offset in tables
-    size_t select_smem = 0;
+    int priority = 0;          // launch priority (largest windows highest)
+    size_t tiles_first = 0;    // first distance tile (triple) of this class
+    size_t n_tiles = 0;
+    std::vector<CoreLaunch> cores;
 };
 
 }  // namespace
@@ -74,8 +84,7 @@ struct hdb_plan {
     std::vector<int64_t> offsets;
     const hdb::PrecisionKernels* k = nullptr;
     std::vector<WindowClass> classes;
-    std::vector<CoreLaunch> cores;
-    std::vector<int32_t> tiles;             // (window, ti, tj)
+    std::vector<int32_t> tiles;             // (window, ti, tj), grouped by class
     std::vector<int64_t> dist_offsets;      // per window (elements), -1 if not materialized
     int64_t dist_elems = 0;
     // Table layout (byte offsets within the workspace).
@@ -83,8 +92,8 @@ struct hdb_plan {
     size_t tables_bytes = 0;
     size_t w_core = 0, w_core_nbr = 0, w_dist = 0, ws_bytes = 0;
     unsigned char* h_tables = nullptr;      // pinned
-    std::vector<cudaStream_t> aux;
-    std::vector<cudaEvent_t> events;
+    std::vector<cudaStream_t> aux;          // one per class (empty: everything on the caller's stream)
+    std::vector<cudaEvent_t> events;        // [2i] class i inputs ready, [2i+1] class i done
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -115,7 +124,7 @@ cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise
 
 // Autotune rules: the first rule whose (precision, core mode, n, D) bounds
 // match a window picks its variant (Prim threads, slots per thread, register
-// dimensions; dims 0 = matrix variant).  The compiled-in defaults below are
+// dimensions; dims 0 = matrix variant; CTAs per window, 1 = single CTA).  The compiled-in defaults below are
 // replaced at run time by hdb_set_tuning (the package loads the table that
 // hdbscan_gb300/autotune.py measured).  A rule naming a variant that is not
 // compiled falls through to the next rule, and the shape heuristic backs up
@@ -128,7 +137,9 @@ struct TuningRule {
     int threads;
     int slots;
     int dims;       // register dimensions; 0 = matrix variant
+    int cluster;    // CTAs per window (thread-block cluster size); 1 = single CTA
 };
+constexpr int kRuleFields = 8;
 
 std::mutex g_tuning_mutex;
 std::vector<TuningRule> g_tuning;  // empty = defaults
@@ -143,10 +154,12 @@ void class_shape(int n, int* threads, int* v) {
     else { *threads = 512; *v = 8; }
 }
 
-const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int threads, int v, int dp) {
-    for (int i = 0; i < k.n_forward; ++i) {
-        const hdb::ForwardVariant& f = k.forward[i];
-        if (f.threads == threads && f.v == v && f.dp == dp) return &f;
+const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int threads, int v, int dp, int cluster = 1) {
+    const hdb::ForwardVariant* list = cluster > 1 ? k.cluster : k.forward;
+    const int count = cluster > 1 ? k.n_cluster : k.n_forward;
+    for (int i = 0; i < count; ++i) {
+        const hdb::ForwardVariant& f = list[i];
+        if (f.threads == threads && f.v == v && f.dp == dp && f.cluster == cluster) return &f;
     }
     return nullptr;
 }
@@ -160,15 +173,26 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
         std::lock_guard<std::mutex> lock(g_tuning_mutex);
         for (const TuningRule& r : g_tuning) {
             if ((r.precision >= 0 && r.precision != precision) || (r.unit >= 0 && r.unit != (unit ? 1 : 0)) ||
-                n > r.n_max || D > r.d_max || r.threads * r.slots < n || (r.dims > 0 && D > r.dims))
+                n > r.n_max || D > r.d_max || r.threads * r.slots * r.cluster < n || (r.dims > 0 && D > r.dims))
                 continue;
-            const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims);
+            const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims, r.cluster);
             if (f) return f;
         }
     }
-    // Defaults.  float64 SIMT is a small fraction of float32 on GB300, so
-    // float64 windows use the matrix variant: the distance block is computed
-    // once per pair by a grid spread over every SM, and Prim only reads rows.
+    // Defaults.  float32 windows above 1024 points with D <= 32 spread their
+    // Prim over a cluster of 2 or 4 CTAs (1024 register-resident vertices per
+    // CTA).  float64 SIMT is a small fraction of float32 on GB300, so float64
+    // windows use the matrix variant: the distance block is computed once per
+    // pair by a grid spread over every SM, and Prim only reads rows.
+    if (precision == HDB_F32 && n > 1024 && D <= 32) {
+        const int cluster = n <= 2048 ? 2 : 4;
+        for (int option : {8, 16, 32})
+            if (D <= option) {
+                const hdb::ForwardVariant* f = find_variant(k, 512, 2, option, cluster);
+                if (f) return f;
+                break;
+            }
+    }
     int dp = 0;
     if (precision == HDB_F32) {
         for (int option : {8, 16, 32})
@@ -236,7 +260,7 @@ int build_plan(hdb_plan* p) {
         int rc = smem_budget(fv->func, optin, &budget);
         if (rc) return rc;
         hdb::ForwardLayout layout{};
-        if (!k.forward_layout(n, fv->dp, unit, budget, &layout))
+        if (!fv->layout(n, unit, budget, &layout))
             return fail(HDB_E_INVALID, "window of " + std::to_string(n) + " points exceeds shared memory");
         WindowClass* cls = nullptr;
         for (auto& c : p->classes)
@@ -258,6 +282,7 @@ int build_plan(hdb_plan* p) {
     p->dist_offsets.assign(p->B, -1);
     p->dist_elems = 0;
     for (auto& c : p->classes) {
+        c.tiles_first = p->tiles.size() / 3;
         if (c.fv->dp != 0) continue;
         for (int w : c.windows) {
             const int n = size_of(w);
@@ -272,34 +297,30 @@ int build_plan(hdb_plan* p) {
                     p->tiles.push_back(tj);
                 }
         }
+        c.n_tiles = p->tiles.size() / 3 - c.tiles_first;
     }
 
     // ---- core distances -----------------------------------------------------
     if (!unit) {
-        for (int pass = 0; pass < 2; ++pass) {
-            const bool matrix = pass == 1;
+        for (auto& c : p->classes) {
+            const bool matrix = c.fv->dp == 0;
             CoreLaunch launch;
             launch.matrix = matrix;
             launch.cv = choose_core(k, p->precision, p->ms, p->D, matrix);
             CoreLaunch select;
             select.matrix = matrix;
-            int nmax = 0;
-            for (auto& c : p->classes) {
-                if ((c.fv->dp == 0) != matrix) continue;
-                for (int w : c.windows) {
-                    const int n = size_of(w);
-                    nmax = std::max(nmax, n);
-                    if (launch.cv) {
-                        for (int r = 0; r < n; r += 128) { launch.items.push_back(w); launch.items.push_back(r); }
-                    } else {
-                        for (int r = 0; r < n; ++r) { select.items.push_back(w); select.items.push_back(r); }
-                    }
+            for (int w : c.windows) {
+                const int n = size_of(w);
+                if (launch.cv) {
+                    for (int r = 0; r < n; r += 128) { launch.items.push_back(w); launch.items.push_back(r); }
+                } else {
+                    for (int r = 0; r < n; ++r) { select.items.push_back(w); select.items.push_back(r); }
                 }
             }
-            if (!launch.items.empty()) p->cores.push_back(launch);
+            if (!launch.items.empty()) c.cores.push_back(launch);
             if (!select.items.empty()) {
-                select.select_smem = (size_t)nmax * (size_t)real_bytes(p->precision);
-                p->cores.push_back(select);
+                select.select_smem = (size_t)c.nmax * (size_t)real_bytes(p->precision);
+                c.cores.push_back(select);
             }
         }
     }
@@ -309,18 +330,40 @@ int build_plan(hdb_plan* p) {
         size_t budget = 0;
         int rc = smem_budget(c.fv->func, optin, &budget);
         if (rc) return rc;
-        if (!k.forward_layout(c.nmax, c.fv->dp, unit, budget, &c.layout) || c.layout.n_arenas != c.n_arenas ||
+        if (!c.fv->layout(c.nmax, unit, budget, &c.layout) || c.layout.n_arenas != c.n_arenas ||
             c.layout.x_in_smem != c.x_in_smem)
             return fail(HDB_E_INVALID, "inconsistent shared-memory layout for a window class");
         c.smem = c.layout.bytes;
         HDB_CUDA(raise_smem_limit(c.fv->func, c.smem));
-        int per_sm = 0;
-        HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads + 32, c.smem));
-        if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
-        c.grid = (int)std::min<size_t>(c.windows.size(), (size_t)per_sm * p->sms);
+        if (c.fv->cluster > 1) {
+            // Persistent clusters: as many as can be co-resident, at most one per window.
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)(c.fv->cluster * std::max<size_t>(c.windows.size(), 1)));
+            cfg.blockDim = dim3((unsigned)(c.fv->threads + 32));
+            cfg.dynamicSmemBytes = c.smem;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = (unsigned)c.fv->cluster;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            HDB_CUDA(cudaOccupancyMaxActiveClusters(&clusters, c.fv->func, &cfg));
+            if (clusters < 1) return fail(HDB_E_INVALID, "cluster forward kernel variant cannot be resident");
+            if (p->flags & HDB_FLAG_ONE_PERSISTENT) clusters = 1;
+            c.grid = c.fv->cluster * (int)std::min<size_t>(c.windows.size(), (size_t)clusters);
+        } else {
+            int per_sm = 0;
+            HDB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.fv->func, c.fv->threads + 32, c.smem));
+            if (per_sm < 1) return fail(HDB_E_INVALID, "forward kernel variant cannot be resident");
+            c.grid = (p->flags & HDB_FLAG_ONE_PERSISTENT) ? 1
+                                                          : (int)std::min<size_t>(c.windows.size(), (size_t)per_sm * p->sms);
+        }
     }
-    for (auto& c : p->cores)
-        if (!c.cv && c.select_smem > 48 * 1024) HDB_CUDA(raise_smem_limit(k.select_func, c.select_smem));
+    for (auto& cls : p->classes)
+        for (auto& c : cls.cores)
+            if (!c.cv && c.select_smem > 48 * 1024) HDB_CUDA(raise_smem_limit(k.select_func, c.select_smem));
 
     // ---- table image --------------------------------------------------------
     std::vector<unsigned char> image;
@@ -338,7 +381,8 @@ int build_plan(hdb_plan* p) {
     p->t_queue = put(image, cursor, queue);
     p->t_tickets = put(image, cursor, tickets);
     p->t_tiles = put(image, cursor, p->tiles);
-    for (auto& c : p->cores) c.items_off = put(image, cursor, c.items);
+    for (auto& cls : p->classes)
+        for (auto& c : cls.cores) c.items_off = put(image, cursor, c.items);
     std::vector<int32_t> edge_window;
     edge_window.reserve((size_t)(p->T - p->B));
     for (int w = 0; w < p->B; ++w)
@@ -363,12 +407,16 @@ int build_plan(hdb_plan* p) {
     // ---- streams for concurrent classes ------------------------------------
     const bool fork = !(p->flags & HDB_FLAG_NO_GRAPH_STREAMS) && p->classes.size() > 1;
     if (fork) {
-        for (size_t i = 1; i < p->classes.size(); ++i) {
+        int least = 0, greatest = 0;  // numerically: greatest <= least
+        HDB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        for (size_t i = 0; i < p->classes.size(); ++i) {
             cudaStream_t s;
-            HDB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            const int priority = std::min(least, greatest + (int)i);
+            p->classes[i].priority = priority;
+            HDB_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority));
             p->aux.push_back(s);
         }
-        for (size_t i = 0; i < p->classes.size(); ++i) {
+        for (size_t i = 0; i < 2 * p->classes.size(); ++i) {
             cudaEvent_t e;
             HDB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             p->events.push_back(e);
@@ -412,43 +460,51 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
     void* core = ex->core ? ex->core : (void*)(ws + p->w_core);
     int32_t* core_nbr = ex->core_nbr ? ex->core_nbr : reinterpret_cast<int32_t*>(ws + p->w_core_nbr);
 
-    if (!p->tiles.empty()) {
-        hdb::DistanceArgs a{};
-        a.X = X;
-        a.offsets = d_offsets;
-        a.tiles = reinterpret_cast<const int32_t*>(ws + p->t_tiles);
-        a.n_tiles = (int)(p->tiles.size() / 3);
-        a.D = p->D;
-        a.dist = dist;
-        a.dist_offsets = d_dist_off;
-        a.status = status;
-        k.launch_distance(a, a.n_tiles, stream);
-        HDB_CUDA(cudaGetLastError());
-    }
-    for (const auto& c : p->cores) {
-        hdb::CoreArgs a{};
-        a.X = X;
-        a.offsets = d_offsets;
-        a.items = reinterpret_cast<const int32_t*>(ws + c.items_off);
-        a.n_items = (int)(c.items.size() / 2);
-        a.D = p->D;
-        a.ms = p->ms;
-        a.dist = c.matrix ? dist : nullptr;
-        a.dist_offsets = d_dist_off;
-        a.core = core;
-        a.core_nbr = core_nbr;
-        a.status = status;
-        if (c.cv) c.cv->launch(a, a.n_items, stream);
-        else k.launch_select(a, a.n_items, c.select_smem, stream);
-        HDB_CUDA(cudaGetLastError());
-    }
+    if (ex->link_lr && (!ex->link_w || !ex->link_size)) return fail(HDB_E_INVALID, "link_lr needs link_w and link_size");
+    if (ex->edges_uv && !ex->edge_w) return fail(HDB_E_INVALID, "edges_uv needs edge_w");
+    if (ex->cl_parent && (!ex->cl_birth || !ex->cl_stability || !ex->cl_selected || !ex->point_parent || !ex->n_clusters))
+        return fail(HDB_E_INVALID, "cl_parent needs cl_birth, cl_stability, cl_selected, point_parent, n_clusters");
+
     const bool fork = !p->aux.empty();
-    if (fork) {
-        HDB_CUDA(cudaEventRecord(p->events[0], stream));
-        for (auto s : p->aux) HDB_CUDA(cudaStreamWaitEvent(s, p->events[0], 0));
-    }
     for (size_t i = 0; i < p->classes.size(); ++i) {
         const WindowClass& c = p->classes[i];
+        // 1. distance blocks of this class's matrix-variant windows (caller's stream)
+        if (c.n_tiles) {
+            hdb::DistanceArgs a{};
+            a.X = X;
+            a.offsets = d_offsets;
+            a.tiles = reinterpret_cast<const int32_t*>(ws + p->t_tiles) + 3 * c.tiles_first;
+            a.n_tiles = (int)c.n_tiles;
+            a.D = p->D;
+            a.dist = dist;
+            a.dist_offsets = d_dist_off;
+            a.status = status;
+            HDB_CUDA(k.launch_distance(a, a.n_tiles, stream, c.priority));
+        }
+        // 2. core distances of its windows (caller's stream)
+        for (const auto& cl : c.cores) {
+            hdb::CoreArgs a{};
+            a.X = X;
+            a.offsets = d_offsets;
+            a.items = reinterpret_cast<const int32_t*>(ws + cl.items_off);
+            a.n_items = (int)(cl.items.size() / 2);
+            a.D = p->D;
+            a.ms = p->ms;
+            a.dist = cl.matrix ? dist : nullptr;
+            a.dist_offsets = d_dist_off;
+            a.core = core;
+            a.core_nbr = core_nbr;
+            a.status = status;
+            if (cl.cv) HDB_CUDA(cl.cv->launch(a, a.n_items, stream, c.priority));
+            else HDB_CUDA(k.launch_select(a, a.n_items, cl.select_smem, stream, c.priority));
+        }
+        cudaStream_t s = stream;
+        if (fork) {
+            s = p->aux[i];
+            HDB_CUDA(cudaEventRecord(p->events[2 * i], stream));
+            HDB_CUDA(cudaStreamWaitEvent(s, p->events[2 * i], 0));
+        }
+        // 3. the persistent forward over its queue
         hdb::ForwardArgs a{};
         a.X = X;
         a.offsets = d_offsets;
@@ -475,8 +531,6 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.link_lr = ex->link_lr;
         a.link_w = ex->link_w;
         a.link_size = ex->link_size;
-        if (a.link_lr && (!a.link_w || !a.link_size)) return fail(HDB_E_INVALID, "link_lr needs link_w and link_size");
-        if (a.edges_uv && !a.edge_w) return fail(HDB_E_INVALID, "edges_uv needs edge_w");
         a.n_clusters = ex->n_clusters;
         a.cl_parent = ex->cl_parent;
         a.cl_birth = ex->cl_birth;
@@ -484,18 +538,11 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.cl_selected = ex->cl_selected;
         a.point_parent = ex->point_parent;
         a.stage_ns = ex->stage_ns;
-        if (a.cl_parent && (!a.cl_birth || !a.cl_stability || !a.cl_selected || !a.point_parent || !a.n_clusters))
-            return fail(HDB_E_INVALID, "cl_parent needs cl_birth, cl_stability, cl_selected, point_parent, n_clusters");
-        cudaStream_t s = (fork && i > 0) ? p->aux[i - 1] : stream;
-        c.fv->launch(a, c.grid, c.smem, s);
-        HDB_CUDA(cudaGetLastError());
+        HDB_CUDA(c.fv->launch(a, c.grid, c.smem, s, c.priority));
+        if (fork) HDB_CUDA(cudaEventRecord(p->events[2 * i + 1], s));
     }
-    if (fork) {
-        for (size_t i = 1; i < p->classes.size(); ++i) {
-            HDB_CUDA(cudaEventRecord(p->events[i], p->aux[i - 1]));
-            HDB_CUDA(cudaStreamWaitEvent(stream, p->events[i], 0));
-        }
-    }
+    if (fork)
+        for (size_t i = 0; i < p->classes.size(); ++i) HDB_CUDA(cudaStreamWaitEvent(stream, p->events[2 * i + 1], 0));
     return HDB_OK;
 }
 
@@ -554,13 +601,14 @@ extern "C" {
 int hdb_version(void) { return HDB_VERSION; }
 
 int hdb_set_tuning(const int32_t* rules, int n_rules) {
-    if (n_rules < 0 || (n_rules > 0 && !rules)) return fail(HDB_E_INVALID, "tuning rules must be a [n, 7] int32 array");
+    if (n_rules < 0 || (n_rules > 0 && !rules)) return fail(HDB_E_INVALID, "tuning rules must be a [n, 8] int32 array");
     std::vector<TuningRule> table;
     for (int i = 0; i < n_rules; ++i) {
-        const int32_t* r = rules + 7 * i;
-        TuningRule t{r[0], r[1], r[2], r[3], r[4], r[5], r[6]};
+        const int32_t* r = rules + kRuleFields * i;
+        TuningRule t{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]};
         if (t.precision < -1 || t.precision > 1 || t.unit < -1 || t.unit > 1 || t.n_max < 2 || t.d_max < 1 ||
-            t.threads < 32 || t.threads % 32 || t.threads > 992 || t.slots < 1 || t.dims < 0)
+            t.threads < 32 || t.threads % 32 || t.threads > 992 || t.slots < 1 || t.dims < 0 || t.cluster < 1 ||
+            t.cluster > 8)
             return fail(HDB_E_INVALID, "tuning rule " + std::to_string(i) + " is out of range");
         table.push_back(t);
     }
@@ -572,12 +620,15 @@ int hdb_set_tuning(const int32_t* rules, int n_rules) {
 int hdb_list_variants(int precision, int32_t* out, int capacity) {
     if (precision != HDB_F32 && precision != HDB_F64) return fail(HDB_E_INVALID, "precision must be 'float32' or 'float64'");
     const hdb::PrecisionKernels& k = precision == HDB_F32 ? hdb::kernels_f32() : hdb::kernels_f64();
-    for (int i = 0; i < k.n_forward && i < capacity && out; ++i) {
-        out[3 * i] = k.forward[i].threads;
-        out[3 * i + 1] = k.forward[i].v;
-        out[3 * i + 2] = k.forward[i].dp;
+    const int total = k.n_forward + k.n_cluster;
+    for (int i = 0; i < total && i < capacity && out; ++i) {
+        const hdb::ForwardVariant& f = i < k.n_forward ? k.forward[i] : k.cluster[i - k.n_forward];
+        out[4 * i] = f.threads;
+        out[4 * i + 1] = f.v;
+        out[4 * i + 2] = f.dp;
+        out[4 * i + 3] = f.cluster;
     }
-    return k.n_forward;
+    return total;
 }
 
 int hdb_get_tuning(int32_t* rules, int capacity) {
@@ -585,8 +636,8 @@ int hdb_get_tuning(int32_t* rules, int capacity) {
     const int count = (int)g_tuning.size();
     for (int i = 0; i < count && i < capacity && rules; ++i) {
         const TuningRule& t = g_tuning[i];
-        const int32_t v[7] = {t.precision, t.unit, t.n_max, t.d_max, t.threads, t.slots, t.dims};
-        for (int j = 0; j < 7; ++j) rules[7 * i + j] = v[j];
+        const int32_t v[kRuleFields] = {t.precision, t.unit, t.n_max, t.d_max, t.threads, t.slots, t.dims, t.cluster};
+        for (int j = 0; j < kRuleFields; ++j) rules[kRuleFields * i + j] = v[j];
     }
     return count;
 }
@@ -663,20 +714,23 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
         const auto& c = p->classes[i];
         s += (i ? "," : "") + std::string("{\"threads\":") + std::to_string(c.fv->threads) +
              ",\"vertices_per_thread\":" + std::to_string(c.fv->v) + ",\"register_dims\":" +
-             std::to_string(c.fv->dp) + ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
+             std::to_string(c.fv->dp) + ",\"cluster\":" + std::to_string(c.fv->cluster) +
+             ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
              "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
              ",\"windows\":" +
              std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
              std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";
     }
     s += "],\"core\":[";
-    for (size_t i = 0; i < p->cores.size(); ++i) {
-        const auto& c = p->cores[i];
-        s += (i ? "," : "") + std::string("{\"kernel\":\"") +
-             (c.cv ? (c.matrix ? "core_matrix" : "core_points") : "core_select") + "\",\"k\":" +
-             std::to_string(c.cv ? c.cv->k : 0) + ",\"register_dims\":" + std::to_string(c.cv ? c.cv->dp : 0) +
-             ",\"items\":" + std::to_string(c.items.size() / 2) + "}";
-    }
+    bool first = true;
+    for (const auto& cls : p->classes)
+        for (const auto& c : cls.cores) {
+            s += (first ? "" : ",") + std::string("{\"kernel\":\"") +
+                 (c.cv ? (c.matrix ? "core_matrix" : "core_points") : "core_select") + "\",\"k\":" +
+                 std::to_string(c.cv ? c.cv->k : 0) + ",\"register_dims\":" + std::to_string(c.cv ? c.cv->dp : 0) +
+                 ",\"items\":" + std::to_string(c.items.size() / 2) + "}";
+            first = false;
+        }
     s += "]}";
     if (s.size() + 1 > size) return fail(HDB_E_INVALID, "describe buffer too small");
     std::memcpy(buffer, s.c_str(), s.size() + 1);
@@ -763,8 +817,7 @@ int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, con
     a.core = ex->core;
     a.core_nbr = ex->core_nbr;
     a.dX = dX;
-    if (a.n_edges > 0) p->k->launch_backward(a, (a.n_edges + 255) / 256, s);
-    HDB_CUDA(cudaGetLastError());
+    if (a.n_edges > 0) HDB_CUDA(p->k->launch_backward(a, (a.n_edges + 255) / 256, s, 0));
     return HDB_OK;
 }
 

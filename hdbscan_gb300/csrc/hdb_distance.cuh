@@ -77,13 +77,21 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
         for (int b = 0; b < 4; ++b) acc[a][b] = Real(0);
 
     for (int k0 = 0; k0 < D; k0 += KC) {
-        // Stage [64 rows x KC coords] of each block, transposed to [KC][64].
-        for (int t = tid; t < kDistTile * KC; t += 256) {
-            const int r = t / KC, k = t - r * KC;
-            const int gk = k0 + k;
+        // Stage [64 rows x KC coords] of each block, transposed to [KC][64]:
+        // lanes walk the row index, so each shared store instruction writes
+        // consecutive words (no bank conflicts); every thread covers KC/4
+        // coordinates of one row (row reads hit L1/L2: the window is reused
+        // by every tile of its block row).
+        {
+            constexpr int KQ = KC / 4;
+            const int r = tid & (kDistTile - 1), kq = tid >> 6;
             const int gi = i0 + r, gj = j0 + r;
-            s_i[k][r] = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : Real(0);
-            s_j[k][r] = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : Real(0);
+#pragma unroll
+            for (int kk = 0; kk < KQ; ++kk) {
+                const int k = kq * KQ + kk, gk = k0 + k;
+                s_i[k][r] = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : Real(0);
+                s_j[k][r] = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : Real(0);
+            }
         }
         __syncthreads();
         const int kend = min(KC, D - k0);
@@ -136,6 +144,7 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
 // ---------------------------------------------------------------------------
 
 constexpr int kCoreRows = 128;
+constexpr int kCorePrefetch = 16;
 
 // Insert (d, j) into the ascending register list L/LI of length K; strict '<'
 // keeps earlier (smaller) indices ahead among equal values.
@@ -242,7 +251,17 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_matrix_kernel(const CoreAr
     int LI[K];
 #pragma unroll
     for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
-    for (int j = 0; j < n; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + j * ld + i), j);
+    // kCorePrefetch independent row loads in flight per thread: the pass is
+    // bound by memory latency, not by the insertions.
+    int j0 = 0;
+    for (; j0 + kCorePrefetch <= n; j0 += kCorePrefetch) {
+        Real v[kCorePrefetch];
+#pragma unroll
+        for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
+#pragma unroll
+        for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
+    }
+    for (int j = j0; j < n; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
     Real value = Real(0);
     int index = -1;
     topk_pick<Real, K>(L, LI, args.ms - 1, value, index);

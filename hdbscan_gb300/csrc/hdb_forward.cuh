@@ -293,6 +293,69 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
     return overflow;
 }
 
+// The hierarchy of one window by the tree warp: exports of the Prim edges,
+// NumPy-order sort, linkage, condensation, selection and labels
+// (reference _kernels.py:358-760), on the arena at `base`.
+template <typename Real>
+__device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char* base_ptr, int w, int n) {
+    const int lane = threadIdx.x & 31;
+    const Real epsilon = (Real)args.eps;  // the reference casts options to Real (_cuda.py:105)
+    const int m = n - 1;
+    if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 3] = global_ns();
+    const int64_t base = args.offsets[w];
+    const int64_t ebase = base - w;
+    Arena<Real> a = Arena<Real>::carve(base_ptr, n);
+    if (args.edges_uv) {
+        for (int i = lane; i < m; i += 32) {
+            args.edges_uv[2 * (ebase + i)] = a.s0[i];
+            args.edges_uv[2 * (ebase + i) + 1] = a.s1[i];
+            static_cast<Real*>(args.edge_w)[ebase + i] = a.r0[i];
+        }
+    }
+    sort_edges_warp<Real>(a, m);
+    if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
+    if (args.order)
+        for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
+        const int e = a.s2[i];
+        const int16_t u = a.s0[e], v = a.s1[e];
+        a.s2[i] = u;
+        a.s3[i] = v;
+    }
+    __syncwarp();
+    linkage_warp<Real>(a, n);
+    if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 5] = global_ns();
+    if (args.link_lr) {
+        for (int i = lane; i < m; i += 32) {
+            args.link_lr[2 * (ebase + i)] = a.s4[i];
+            args.link_lr[2 * (ebase + i) + 1] = a.s5[i];
+            args.link_size[ebase + i] = a.s6[i];
+            static_cast<Real*>(args.link_w)[ebase + i] = a.r0[i];
+        }
+    }
+    __syncwarp();
+    const int next_label = condense_warp<Real>(a, n, args.mcs);
+    if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
+    if (args.cl_parent) {
+        for (int c = lane; c < next_label - n; c += 32) {
+            args.cl_parent[base + c] = a.s2[c];
+            static_cast<Real*>(args.cl_birth)[base + c] = a.r1[c];
+        }
+    }
+    __syncwarp();
+    select_and_label_warp<Real>(a, n, next_label, epsilon, args.labels + base);
+    if (args.cl_parent) {
+        for (int c = lane; c < next_label - n; c += 32) {
+            static_cast<Real*>(args.cl_stability)[base + c] = a.r2[c];
+            args.cl_selected[base + c] = a.sel[c];
+        }
+        for (int i = lane; i < n; i += 32) args.point_parent[base + i] = a.s9[i];
+        if (lane == 0) args.n_clusters[w] = next_label - n;
+    }
+    if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 7] = global_ns();
+}
+
 struct WindowMeta {
     int w;      // window index, -1 = queue exhausted
     int n;
@@ -302,7 +365,7 @@ struct WindowMeta {
 // Dynamic shared memory: n_arenas arenas of arena_stride bytes, then the
 // staged window (x_off) and its core distances (core_off); see the plan layer.
 template <typename Real, int PT, int SV, int DP>
-__global__ void __launch_bounds__(PT + 32, 1) hdb_forward_kernel(const ForwardArgs args) {
+__global__ void __launch_bounds__(PT + 32, 1) hdb_forward_kernel(const __grid_constant__ ForwardArgs args) {
     using T = RealTraits<Real>;
     using Key = typename T::Bits;
     constexpr int PW = PT / 32;
@@ -330,68 +393,12 @@ __global__ void __launch_bounds__(PT + 32, 1) hdb_forward_kernel(const ForwardAr
 
     if (warp == PW) {
         // =================== tree warp (consumer) ============================
-        const Real epsilon = (Real)args.eps;  // the reference casts options to Real (_cuda.py:105)
         for (int k = 0; k < (1 << 30); ++k) {
             const int b = nb == 2 ? (k & 1) : 0;
             bar_sync(kBarFull + b, PT + 32);
             const WindowMeta meta = s_meta[b];
             if (meta.w < 0) return;
-            if (!meta.skip) {
-                const int w = meta.w, n = meta.n, m = n - 1;
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 3] = global_ns();
-                const int64_t base = args.offsets[w];
-                const int64_t ebase = base - w;
-                Arena<Real> a = Arena<Real>::carve(smem + (size_t)b * args.arena_stride, n);
-                if (args.edges_uv) {
-                    for (int i = lane; i < m; i += 32) {
-                        args.edges_uv[2 * (ebase + i)] = a.s0[i];
-                        args.edges_uv[2 * (ebase + i) + 1] = a.s1[i];
-                        static_cast<Real*>(args.edge_w)[ebase + i] = a.r0[i];
-                    }
-                }
-                sort_edges_warp<Real>(a, m);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
-                if (args.order)
-                    for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
-                __syncwarp();
-                for (int i = lane; i < m; i += 32) {
-                    const int e = a.s2[i];
-                    const int16_t u = a.s0[e], v = a.s1[e];
-                    a.s2[i] = u;
-                    a.s3[i] = v;
-                }
-                __syncwarp();
-                linkage_warp<Real>(a, n);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 5] = global_ns();
-                if (args.link_lr) {
-                    for (int i = lane; i < m; i += 32) {
-                        args.link_lr[2 * (ebase + i)] = a.s4[i];
-                        args.link_lr[2 * (ebase + i) + 1] = a.s5[i];
-                        args.link_size[ebase + i] = a.s6[i];
-                        static_cast<Real*>(args.link_w)[ebase + i] = a.r0[i];
-                    }
-                }
-                __syncwarp();
-                const int next_label = condense_warp<Real>(a, n, args.mcs);
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
-                if (args.cl_parent) {
-                    for (int c = lane; c < next_label - n; c += 32) {
-                        args.cl_parent[base + c] = a.s2[c];
-                        static_cast<Real*>(args.cl_birth)[base + c] = a.r1[c];
-                    }
-                }
-                __syncwarp();
-                select_and_label_warp<Real>(a, n, next_label, epsilon, args.labels + base);
-                if (args.cl_parent) {
-                    for (int c = lane; c < next_label - n; c += 32) {
-                        static_cast<Real*>(args.cl_stability)[base + c] = a.r2[c];
-                        args.cl_selected[base + c] = a.sel[c];
-                    }
-                    for (int i = lane; i < n; i += 32) args.point_parent[base + i] = a.s9[i];
-                    if (lane == 0) args.n_clusters[w] = next_label - n;
-                }
-                if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 7] = global_ns();
-            }
+            if (!meta.skip) tree_window<Real>(args, smem + (size_t)b * args.arena_stride, meta.w, meta.n);
             __syncwarp();
             __threadfence_block();
             bar_arrive(kBarEmpty + b, PT + 32);

@@ -4,29 +4,38 @@
 #include "hdb_backward.cuh"
 #include "hdb_distance.cuh"
 #include "hdb_forward.cuh"
+#include "hdb_launch.h"
 #include "hdb_registry.h"
 
 namespace hdb {
 
+template <typename Real>
+bool forward_layout(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out);
+
 template <typename Real, int THREADS, int V, int DP>
-void launch_forward(const ForwardArgs& a, int grid, size_t smem, cudaStream_t s) {
-    hdb_forward_kernel<Real, THREADS, V, DP><<<grid, THREADS + 32, smem, s>>>(a);
+cudaError_t launch_forward(const ForwardArgs& a, int grid, size_t smem, cudaStream_t s, int priority) {
+    return launch_ex(hdb_forward_kernel<Real, THREADS, V, DP>, grid, THREADS + 32, smem, s, priority, 1, a);
+}
+
+template <typename Real, int DP>
+bool single_layout(int n, bool unit_core, size_t budget, ForwardLayout* out) {
+    return forward_layout<Real>(n, DP, unit_core, budget, out);
 }
 
 template <typename Real, int THREADS, int V, int DP>
 constexpr ForwardVariant forward_variant() {
-    return ForwardVariant{THREADS, V, DP, (const void*)hdb_forward_kernel<Real, THREADS, V, DP>,
-                          launch_forward<Real, THREADS, V, DP>};
+    return ForwardVariant{THREADS, V, DP, 1, (const void*)hdb_forward_kernel<Real, THREADS, V, DP>,
+                          launch_forward<Real, THREADS, V, DP>, single_layout<Real, DP>};
 }
 
 template <typename Real, int K, int DP>
-void launch_core_points(const CoreArgs& a, int grid, cudaStream_t s) {
-    hdb_core_points_kernel<Real, K, DP><<<grid, kCoreRows, 0, s>>>(a);
+cudaError_t launch_core_points(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
+    return launch_ex(hdb_core_points_kernel<Real, K, DP>, grid, kCoreRows, 0, s, priority, 1, a);
 }
 
 template <typename Real, int K>
-void launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s) {
-    hdb_core_matrix_kernel<Real, K><<<grid, kCoreRows, 0, s>>>(a);
+cudaError_t launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
+    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreRows, 0, s, priority, 1, a);
 }
 
 template <typename Real, int K, int DP>
@@ -40,18 +49,18 @@ constexpr CoreVariant core_matrix_variant() {
 }
 
 template <typename Real>
-void launch_distance(const DistanceArgs& a, int grid, cudaStream_t s) {
-    hdb_distance_kernel<Real><<<grid, 256, 0, s>>>(a);
+cudaError_t launch_distance(const DistanceArgs& a, int grid, cudaStream_t s, int priority) {
+    return launch_ex(hdb_distance_kernel<Real>, grid, 256, 0, s, priority, 1, a);
 }
 
 template <typename Real>
-void launch_select(const CoreArgs& a, int grid, size_t smem, cudaStream_t s) {
-    hdb_core_select_kernel<Real><<<grid, 256, smem, s>>>(a);
+cudaError_t launch_select(const CoreArgs& a, int grid, size_t smem, cudaStream_t s, int priority) {
+    return launch_ex(hdb_core_select_kernel<Real>, grid, 256, smem, s, priority, 1, a);
 }
 
 template <typename Real>
-void launch_backward(const BackwardArgs& a, int grid, cudaStream_t s) {
-    hdb_backward_kernel<Real><<<grid, 256, 0, s>>>(a);
+cudaError_t launch_backward(const BackwardArgs& a, int grid, cudaStream_t s, int priority) {
+    return launch_ex(hdb_backward_kernel<Real>, grid, 256, 0, s, priority, 1, a);
 }
 
 // Two arenas (Prim/tree overlap) when they fit next to the staged window,

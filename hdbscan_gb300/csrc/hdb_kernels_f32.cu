@@ -43,11 +43,17 @@ const CoreVariant kCore[] = {
     core_matrix_variant<float, 8>(),      core_matrix_variant<float, 16>(),
     core_matrix_variant<float, 32>(),     core_matrix_variant<float, 64>(),
 };
-const PrecisionKernels kTable = {
-    4, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), kCore, (int)(sizeof(kCore) / sizeof(kCore[0])),
-    launch_distance<float>, launch_select<float>, (const void*)hdb_core_select_kernel<float>,
-    launch_backward<float>, forward_layout<float>,
-};
 }  // namespace
-const PrecisionKernels& kernels_f32() { return kTable; }
+const PrecisionKernels& kernels_f32() {
+    static const PrecisionKernels table = [] {
+        PrecisionKernels t = {
+            4, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), nullptr, 0, kCore,
+            (int)(sizeof(kCore) / sizeof(kCore[0])), launch_distance<float>, launch_select<float>,
+            (const void*)hdb_core_select_kernel<float>, launch_backward<float>, forward_layout<float>,
+        };
+        t.cluster = cluster_variants_f32(&t.n_cluster);
+        return t;
+    }();
+    return table;
+}
 }  // namespace hdb

@@ -36,11 +36,17 @@ const CoreVariant kCore[] = {
     core_matrix_variant<double, 8>(),      core_matrix_variant<double, 16>(),
     core_matrix_variant<double, 32>(),     core_matrix_variant<double, 64>(),
 };
-const PrecisionKernels kTable = {
-    8, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), kCore, (int)(sizeof(kCore) / sizeof(kCore[0])),
-    launch_distance<double>, launch_select<double>, (const void*)hdb_core_select_kernel<double>,
-    launch_backward<double>, forward_layout<double>,
-};
 }  // namespace
-const PrecisionKernels& kernels_f64() { return kTable; }
+const PrecisionKernels& kernels_f64() {
+    static const PrecisionKernels table = [] {
+        PrecisionKernels t = {
+            8, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), nullptr, 0, kCore,
+            (int)(sizeof(kCore) / sizeof(kCore[0])), launch_distance<double>, launch_select<double>,
+            (const void*)hdb_core_select_kernel<double>, launch_backward<double>, forward_layout<double>,
+        };
+        t.cluster = cluster_variants_f64(&t.n_cluster);
+        return t;
+    }();
+    return table;
+}
 }  // namespace hdb

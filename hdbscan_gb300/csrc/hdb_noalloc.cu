@@ -209,9 +209,8 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
         a.ms = min_samples;
         a.core = core;
         a.status = status;
-        if (cv) cv->launch(a, n_items, stream);
-        else k.launch_select(a, n_items, select_smem, stream);
-        e = cudaGetLastError();
+        if (cv) e = cv->launch(a, n_items, stream, 0);
+        else e = k.launch_select(a, n_items, select_smem, stream, 0);
         if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("core kernel: ") + cudaGetErrorString(e));
     }
 
@@ -234,8 +233,7 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     a.labels = labels;
     a.status = status;
     const int grid = batch < per_sm * sms ? batch : per_sm * sms;
-    fv->launch(a, grid, smem, stream);
-    e = cudaGetLastError();
+    e = fv->launch(a, grid, smem, stream, 0);
     if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("forward kernel: ") + cudaGetErrorString(e));
     return HDB_OK;
 }

@@ -9,6 +9,7 @@
 
 namespace hdb {
 
+// Every launcher takes the launch priority (numerically as stream priorities).
 // Dynamic shared-memory layout of one forward launch.
 struct ForwardLayout {
     int n_arenas;
@@ -23,33 +24,41 @@ struct ForwardVariant {
     int threads;  // Prim threads; the CTA has threads + 32 (one tree warp)
     int v;        // vertices (slots) per Prim thread
     int dp;       // padded register dimensions; 0 = matrix variant
+    int cluster;  // CTAs per window (1 = hdb_forward_kernel, else a cluster of hdb_cluster_forward_kernel)
     const void* func;
-    void (*launch)(const ForwardArgs&, int grid, size_t smem, cudaStream_t);
+    cudaError_t (*launch)(const ForwardArgs&, int grid, size_t smem, cudaStream_t, int priority);
+    // Shared-memory layout for windows of up to n points within `budget` bytes; false if none fits.
+    bool (*layout)(int n, bool unit_core, size_t budget, ForwardLayout* out);
 };
 
 struct CoreVariant {
     int k;        // list length (max ms)
     int dp;       // padded register dimensions; 0 = matrix variant
     const void* func;
-    void (*launch)(const CoreArgs&, int grid, cudaStream_t);
+    cudaError_t (*launch)(const CoreArgs&, int grid, cudaStream_t, int priority);
 };
 
 struct PrecisionKernels {
     int real_bytes;
-    const ForwardVariant* forward;
+    const ForwardVariant* forward;   // single-CTA variants
     int n_forward;
+    const ForwardVariant* cluster;   // cluster variants (windows above 1024 points)
+    int n_cluster;
     const CoreVariant* core;
     int n_core;
-    void (*launch_distance)(const DistanceArgs&, int grid, cudaStream_t);
-    void (*launch_select)(const CoreArgs&, int grid, size_t smem, cudaStream_t);
+    cudaError_t (*launch_distance)(const DistanceArgs&, int grid, cudaStream_t, int priority);
+    cudaError_t (*launch_select)(const CoreArgs&, int grid, size_t smem, cudaStream_t, int priority);
     const void* select_func;
-    void (*launch_backward)(const BackwardArgs&, int grid, cudaStream_t);
-    // Best layout for windows of up to n points within `budget` bytes; false if none fits.
+    cudaError_t (*launch_backward)(const BackwardArgs&, int grid, cudaStream_t, int priority);
+    // Best single-CTA layout for windows of up to n points within `budget` bytes; false if none fits.
     bool (*forward_layout)(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out);
 };
 
 const PrecisionKernels& kernels_f32();
 const PrecisionKernels& kernels_f64();
+// Cluster variants, compiled in their own translation units.
+const ForwardVariant* cluster_variants_f32(int* count);
+const ForwardVariant* cluster_variants_f64(int* count);
 
 // Raise (never lower) a kernel's dynamic shared-memory limit; thread-safe.
 cudaError_t raise_dynamic_smem(const void* func, size_t bytes);

@@ -56,6 +56,8 @@ extern "C" {
 /* Plan flags. */
 #define HDB_FLAG_FORCE_MATRIX 1u /* materialize every window's distance block (matrix Prim) */
 #define HDB_FLAG_NO_GRAPH_STREAMS 2u /* run all window classes on the caller's stream */
+#define HDB_FLAG_ONE_PERSISTENT 4u /* one persistent CTA (or cluster) per window class: every window of a
+                                      class passes through the same CTAs (queue and hand-off tests) */
 
 typedef struct hdb_plan hdb_plan_t;
 
@@ -89,19 +91,21 @@ int hdb_version(void);
 const char* hdb_last_error(void);
 
 /* Autotune table used by later hdb_plan_create calls (process-wide).  Each
- * rule is 7 int32: {precision (HDB_F32/HDB_F64/-1 any), unit core (1 =
+ * rule is 8 int32: {precision (HDB_F32/HDB_F64/-1 any), unit core (1 =
  * min_samples <= 2, 0 = core distances, -1 any), n_max, d_max, Prim threads,
- * slots per thread, register dims (0 = matrix variant)}; the first rule that
- * matches a window and names a compiled variant wins, built-in defaults back
- * it up.  n_rules = 0 restores the defaults.  Replaces the fixed launch choice
- * of hdbscan_gpu/_cuda.py:82-88 (block width, register Prim, shared arena). */
+ * slots per thread, register dims (0 = matrix variant), CTAs per window (1 =
+ * one CTA, 2..8 = a thread-block cluster)}; the first rule that matches a
+ * window and names a compiled variant wins, built-in defaults back it up.
+ * n_rules = 0 restores the defaults.  Replaces the fixed launch choice of
+ * hdbscan_gpu/_cuda.py:82-88 (block width, register Prim, shared arena). */
 int hdb_set_tuning(const int32_t* rules, int n_rules);
 
 /* Copies up to `capacity` rules of the current table; returns their count. */
 int hdb_get_tuning(int32_t* rules, int capacity);
 
 /* Compiled forward variants of a precision as {Prim threads, slots, register
- * dims (0 = matrix)} triples; returns their count (the autotuner's candidates). */
+ * dims (0 = matrix), CTAs per window} quadruples; returns their count (the
+ * autotuner's candidates). */
 int hdb_list_variants(int precision, int32_t* out, int capacity);
 
 /* Build a plan for a ragged batch: `windows` windows whose points are rows
