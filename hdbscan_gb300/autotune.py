@@ -33,11 +33,11 @@ N_BUCKETS = (64, 128, 256, 512, 1024, 2048, 4096)
 D_BUCKETS = (8, 16, 32, 64, 128)
 
 
-FIELDS = 8
+FIELDS = 9
 
 
 def _rules_array(rules):
-    # Tables written before the cluster field existed hold 7-field rules: one CTA.
+    # Older tables hold 7- or 8-field rules: one CTA per window, one CTA per SM.
     rows = [list(r) + [1] * (FIELDS - len(r)) for r in rules]
     return np.ascontiguousarray(np.asarray(rows, dtype=np.int32).reshape(-1, FIELDS))
 
@@ -65,9 +65,9 @@ def apply_table(lib, path: Path | None = None) -> int:
 
 def variants(lib, precision_code):
     count = lib.hdb_list_variants(precision_code, None, 0)
-    out = np.zeros(4 * count, np.int32)
+    out = np.zeros(5 * count, np.int32)
     lib.hdb_list_variants(precision_code, out.ctypes.data_as(ctypes.c_void_p), count)
-    return [tuple(int(v) for v in out[4 * i:4 * i + 4]) for i in range(count)]
+    return [tuple(int(v) for v in out[5 * i:5 * i + 5]) for i in range(count)]
 
 
 def _windows(rng, batch, n, dims):
@@ -128,21 +128,21 @@ def tune(quick=False, out: Path = TABLE, log=print, sizes=None, precisions=None)
                         torch.float32 if precision == "float32" else torch.float64)
                     timings = []
                     reference_labels = None
-                    for threads, slots, dp, cluster in cands:
-                        rule = [code, unit, n, dims, threads, slots, dp, cluster]
+                    for threads, slots, dp, cluster, per_sm in cands:
+                        rule = [code, unit, n, dims, threads, slots, dp, cluster, per_sm]
                         arr = _rules_array([rule])
                         lib.hdb_set_tuning(arr.ctypes.data_as(ctypes.c_void_p), 1)
                         plan = Plan(offsets, dims, min_cluster_size=5, min_samples=ms, precision=precision)
                         desc = json.loads(plan.describe())["classes"][0]
                         if (desc["threads"], desc["vertices_per_thread"], desc["register_dims"],
-                                desc["cluster"]) != (threads, slots, dp, cluster):
+                                desc["cluster"], desc["per_sm"]) != (threads, slots, dp, cluster, per_sm):
                             continue  # the rule was not applicable (e.g. shared memory)
                         ms_time, labels = _time_plan(plan, X, 3 if quick else 5)
                         host = labels.cpu().numpy()
                         if reference_labels is None:
                             reference_labels = host
                         elif not np.array_equal(host, reference_labels):
-                            raise RuntimeError(f"variant {threads}x{slots}/{dp}/c{cluster} changed the labels")
+                            raise RuntimeError(f"variant {threads}x{slots}/{dp}/c{cluster}/s{per_sm} changed the labels")
                         timings.append((ms_time, rule))
                         del plan
                     lib.hdb_set_tuning(None, 0)
@@ -153,7 +153,7 @@ def tune(quick=False, out: Path = TABLE, log=print, sizes=None, precisions=None)
                     records.append({"rule": best, "ms": best_ms, "windows": batch,
                                     "candidates": [{"rule": r, "ms": t} for t, r in timings]})
                     log(f"{precision} unit={unit} n<={n} D<={dims}: {best[4]}x{best[5]} dims={best[6]} "
-                        f"cluster={best[7]} {best_ms:.3f} ms ({len(timings)} candidates)")
+                        f"cluster={best[7]} per_sm={best[8]} {best_ms:.3f} ms ({len(timings)} candidates)")
     if sizes or precisions:
         # Partial re-tune: keep the previous rules of every bucket not measured now.
         measured = {tuple(r["rule"][:4]) for r in records}
@@ -165,7 +165,7 @@ def tune(quick=False, out: Path = TABLE, log=print, sizes=None, precisions=None)
     # Most specific first: smaller n and D buckets are checked before larger ones.
     records.sort(key=lambda r: (r["rule"][0], -r["rule"][1], r["rule"][2], r["rule"][3]))
     table = {"device": torch.cuda.get_device_name(0), "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
-             "fields": ["precision", "unit_core", "n_max", "d_max", "threads", "slots", "dims", "cluster"],
+             "fields": ["precision", "unit_core", "n_max", "d_max", "threads", "slots", "dims", "cluster", "per_sm"],
              "rules": records}
     out.write_text(json.dumps(table, indent=1) + "\n")
     apply_table(lib, out)

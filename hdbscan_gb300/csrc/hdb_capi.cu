@@ -120,11 +120,15 @@ namespace {
 
 int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
 
+constexpr size_t kChunks = 4;     // pipeline depth for large matrix-variant classes
+constexpr size_t kMinChunk = 8;   // windows per chunk at least
+
 cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise_dynamic_smem(func, bytes); }
 
 // Autotune rules: the first rule whose (precision, core mode, n, D) bounds
 // match a window picks its variant (Prim threads, slots per thread, register
-// dimensions; dims 0 = matrix variant; CTAs per window, 1 = single CTA).  The compiled-in defaults below are
+// dimensions; dims 0 = matrix variant; CTAs per window, 1 = single CTA; CTAs
+// per SM).  The compiled-in defaults below are
 // replaced at run time by hdb_set_tuning (the package loads the table that
 // hdbscan_gb300/autotune.py measured).  A rule naming a variant that is not
 // compiled falls through to the next rule, and the shape heuristic backs up
@@ -138,8 +142,9 @@ struct TuningRule {
     int slots;
     int dims;       // register dimensions; 0 = matrix variant
     int cluster;    // CTAs per window (thread-block cluster size); 1 = single CTA
+    int per_sm;     // CTAs per SM of a single-CTA variant (1 or 2)
 };
-constexpr int kRuleFields = 8;
+constexpr int kRuleFields = 9;
 
 std::mutex g_tuning_mutex;
 std::vector<TuningRule> g_tuning;  // empty = defaults
@@ -154,12 +159,13 @@ void class_shape(int n, int* threads, int* v) {
     else { *threads = 512; *v = 8; }
 }
 
-const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int threads, int v, int dp, int cluster = 1) {
+const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int threads, int v, int dp, int cluster = 1,
+                                        int per_sm = 1) {
     const hdb::ForwardVariant* list = cluster > 1 ? k.cluster : k.forward;
     const int count = cluster > 1 ? k.n_cluster : k.n_forward;
     for (int i = 0; i < count; ++i) {
         const hdb::ForwardVariant& f = list[i];
-        if (f.threads == threads && f.v == v && f.dp == dp && f.cluster == cluster) return &f;
+        if (f.threads == threads && f.v == v && f.dp == dp && f.cluster == cluster && f.per_sm == per_sm) return &f;
     }
     return nullptr;
 }
@@ -175,7 +181,7 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
             if ((r.precision >= 0 && r.precision != precision) || (r.unit >= 0 && r.unit != (unit ? 1 : 0)) ||
                 n > r.n_max || D > r.d_max || r.threads * r.slots * r.cluster < n || (r.dims > 0 && D > r.dims))
                 continue;
-            const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims, r.cluster);
+            const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims, r.cluster, r.per_sm);
             if (f) return f;
         }
     }
@@ -202,12 +208,15 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
     return f ? f : find_variant(k, threads, v, 0);
 }
 
-// Dynamic shared memory available to a forward variant next to its static use.
-int smem_budget(const void* func, int optin, size_t* budget) {
+// Dynamic shared memory available to one CTA of a forward variant next to its
+// static use, when `per_sm` CTAs share an SM (each also reserves 1 KB).
+int smem_budget(const hdb::ForwardVariant* fv, int optin, int per_sm_total, size_t* budget) {
     cudaFuncAttributes attr;
-    cudaError_t e = cudaFuncGetAttributes(&attr, func);
+    cudaError_t e = cudaFuncGetAttributes(&attr, fv->func);
     if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
-    *budget = (size_t)optin > attr.sharedSizeBytes + 1024 ? (size_t)optin - attr.sharedSizeBytes - 1024 : 0;
+    size_t limit = (size_t)optin;
+    if (fv->per_sm > 1) limit = std::min(limit, (size_t)per_sm_total / (size_t)fv->per_sm);
+    *budget = limit > attr.sharedSizeBytes + 1024 ? limit - attr.sharedSizeBytes - 1024 : 0;
     return HDB_OK;
 }
 
@@ -243,8 +252,9 @@ int build_plan(hdb_plan* p) {
     const hdb::PrecisionKernels& k = *p->k;
     const bool unit = p->ms <= 2;
     const bool force_matrix = (p->flags & HDB_FLAG_FORCE_MATRIX) != 0;
-    int optin = 0;
+    int optin = 0, per_sm_smem = 0;
     HDB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+    HDB_CUDA(cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
     HDB_CUDA(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
 
     // ---- classes ------------------------------------------------------------
@@ -257,7 +267,7 @@ int build_plan(hdb_plan* p) {
         const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, unit, force_matrix);
         if (!fv) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(n) + " points");
         size_t budget = 0;
-        int rc = smem_budget(fv->func, optin, &budget);
+        int rc = smem_budget(fv, optin, per_sm_smem, &budget);
         if (rc) return rc;
         hdb::ForwardLayout layout{};
         if (!fv->layout(n, unit, budget, &layout))
@@ -274,6 +284,25 @@ int build_plan(hdb_plan* p) {
         }
         cls->windows.push_back(w);
         cls->nmax = std::max(cls->nmax, n);
+    }
+    // Matrix-variant classes with many windows are cut into chunks of the
+    // size-sorted queue: each chunk's Prim loops start once its own distance
+    // blocks exist and overlap the distance work of the next chunk.
+    {
+        std::vector<WindowClass> chunked;
+        for (auto& c : p->classes) {
+            const size_t W = c.windows.size();
+            const size_t parts = (c.fv->dp == 0 && W >= 2 * kMinChunk) ? std::min<size_t>(kChunks, W / kMinChunk) : 1;
+            for (size_t part = 0; part < parts; ++part) {
+                WindowClass piece = c;
+                const size_t lo = W * part / parts, hi = W * (part + 1) / parts;
+                piece.windows.assign(c.windows.begin() + lo, c.windows.begin() + hi);
+                piece.nmax = 0;
+                for (int w : piece.windows) piece.nmax = std::max(piece.nmax, size_of(w));
+                chunked.push_back(std::move(piece));
+            }
+        }
+        p->classes.swap(chunked);
     }
     std::stable_sort(p->classes.begin(), p->classes.end(),
                      [](const WindowClass& a, const WindowClass& b) { return a.nmax > b.nmax; });
@@ -328,7 +357,7 @@ int build_plan(hdb_plan* p) {
     // ---- grids --------------------------------------------------------------
     for (auto& c : p->classes) {
         size_t budget = 0;
-        int rc = smem_budget(c.fv->func, optin, &budget);
+        int rc = smem_budget(c.fv, optin, per_sm_smem, &budget);
         if (rc) return rc;
         if (!c.fv->layout(c.nmax, unit, budget, &c.layout) || c.layout.n_arenas != c.n_arenas ||
             c.layout.x_in_smem != c.x_in_smem)
@@ -601,14 +630,14 @@ extern "C" {
 int hdb_version(void) { return HDB_VERSION; }
 
 int hdb_set_tuning(const int32_t* rules, int n_rules) {
-    if (n_rules < 0 || (n_rules > 0 && !rules)) return fail(HDB_E_INVALID, "tuning rules must be a [n, 8] int32 array");
+    if (n_rules < 0 || (n_rules > 0 && !rules)) return fail(HDB_E_INVALID, "tuning rules must be a [n, 9] int32 array");
     std::vector<TuningRule> table;
     for (int i = 0; i < n_rules; ++i) {
         const int32_t* r = rules + kRuleFields * i;
-        TuningRule t{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7]};
+        TuningRule t{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8]};
         if (t.precision < -1 || t.precision > 1 || t.unit < -1 || t.unit > 1 || t.n_max < 2 || t.d_max < 1 ||
             t.threads < 32 || t.threads % 32 || t.threads > 992 || t.slots < 1 || t.dims < 0 || t.cluster < 1 ||
-            t.cluster > 8)
+            t.cluster > 8 || t.per_sm < 1 || t.per_sm > 4)
             return fail(HDB_E_INVALID, "tuning rule " + std::to_string(i) + " is out of range");
         table.push_back(t);
     }
@@ -623,10 +652,11 @@ int hdb_list_variants(int precision, int32_t* out, int capacity) {
     const int total = k.n_forward + k.n_cluster;
     for (int i = 0; i < total && i < capacity && out; ++i) {
         const hdb::ForwardVariant& f = i < k.n_forward ? k.forward[i] : k.cluster[i - k.n_forward];
-        out[4 * i] = f.threads;
-        out[4 * i + 1] = f.v;
-        out[4 * i + 2] = f.dp;
-        out[4 * i + 3] = f.cluster;
+        out[5 * i] = f.threads;
+        out[5 * i + 1] = f.v;
+        out[5 * i + 2] = f.dp;
+        out[5 * i + 3] = f.cluster;
+        out[5 * i + 4] = f.per_sm;
     }
     return total;
 }
@@ -636,7 +666,8 @@ int hdb_get_tuning(int32_t* rules, int capacity) {
     const int count = (int)g_tuning.size();
     for (int i = 0; i < count && i < capacity && rules; ++i) {
         const TuningRule& t = g_tuning[i];
-        const int32_t v[kRuleFields] = {t.precision, t.unit, t.n_max, t.d_max, t.threads, t.slots, t.dims, t.cluster};
+        const int32_t v[kRuleFields] = {t.precision, t.unit, t.n_max, t.d_max, t.threads, t.slots,
+                                        t.dims,      t.cluster, t.per_sm};
         for (int j = 0; j < kRuleFields; ++j) rules[kRuleFields * i + j] = v[j];
     }
     return count;
@@ -715,6 +746,7 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
         s += (i ? "," : "") + std::string("{\"threads\":") + std::to_string(c.fv->threads) +
              ",\"vertices_per_thread\":" + std::to_string(c.fv->v) + ",\"register_dims\":" +
              std::to_string(c.fv->dp) + ",\"cluster\":" + std::to_string(c.fv->cluster) +
+             ",\"per_sm\":" + std::to_string(c.fv->per_sm) +
              ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
              "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
              ",\"windows\":" +

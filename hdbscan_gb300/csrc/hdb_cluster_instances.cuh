@@ -34,7 +34,7 @@ bool cluster_layout(int n, bool /*unit_core*/, size_t budget, ForwardLayout* out
 
 template <typename Real, int PT, int SV, int DP, int CS>
 constexpr ForwardVariant cluster_variant() {
-    return ForwardVariant{PT, SV, DP, CS, (const void*)hdb_cluster_forward_kernel<Real, PT, SV, DP, CS>,
+    return ForwardVariant{PT, SV, DP, CS, 1, (const void*)hdb_cluster_forward_kernel<Real, PT, SV, DP, CS>,
                           launch_cluster_forward<Real, PT, SV, DP, CS>, cluster_layout<Real, PT, SV, DP, CS>};
 }
 

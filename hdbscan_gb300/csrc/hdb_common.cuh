@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "hdb_args.h"
+#include "hdb_exact.h"
 
 namespace hdb {
 
@@ -23,6 +24,9 @@ template <> struct RealTraits<float> {
     __device__ __forceinline__ static float inf() { return __int_as_float(0x7f800000); }
     __device__ __forceinline__ static float sub(float a, float b) { return __fsub_rn(a, b); }
     __device__ __forceinline__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+    // Correctly rounded a*a of a difference of operand_safe values.
+    __device__ __forceinline__ static float sqr(float a) { return __fmul_rn(a, a); }
+    __device__ __forceinline__ static bool operand_safe(float) { return true; }
     __device__ __forceinline__ static float mul_ru(float a, float b) { return __fmul_ru(a, b); }
     __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
     __device__ __forceinline__ static float sqrt_rn(float a) { return __fsqrt_rn(a); }
@@ -40,6 +44,11 @@ template <> struct RealTraits<double> {
     __device__ __forceinline__ static double inf() { return __longlong_as_double(0x7ff0000000000000ll); }
     __device__ __forceinline__ static double sub(double a, double b) { return __dsub_rn(a, b); }
     __device__ __forceinline__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+    // Correctly rounded a*a of a difference of operand_safe values, on the
+    // integer pipes (hdb_exact.h): the FP64 pipe then carries only the
+    // subtraction and the addition.
+    __device__ __forceinline__ static double sqr(double a) { return sqr_rn_safe(a); }
+    __device__ __forceinline__ static bool operand_safe(double x) { return sqr_operand_safe(x); }
     __device__ __forceinline__ static double mul_ru(double a, double b) { return __dmul_ru(a, b); }
     __device__ __forceinline__ static double add(double a, double b) { return __dadd_rn(a, b); }
     __device__ __forceinline__ static double sqrt_rn(double a) { return __dsqrt_rn(a); }

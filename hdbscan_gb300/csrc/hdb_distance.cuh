@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
         // consecutive words (no bank conflicts); every thread covers KC/4
         // coordinates of one row (row reads hit L1/L2: the window is reused
         // by every tile of its block row).
+        bool safe = true;
         {
             constexpr int KQ = KC / 4;
             const int r = tid & (kDistTile - 1), kq = tid >> 6;
@@ -89,24 +90,33 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
 #pragma unroll
             for (int kk = 0; kk < KQ; ++kk) {
                 const int k = kq * KQ + kk, gk = k0 + k;
-                s_i[k][r] = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : Real(0);
-                s_j[k][r] = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : Real(0);
+                const Real vi = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : Real(0);
+                const Real vj = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : Real(0);
+                safe = safe && T::operand_safe(vi) && T::operand_safe(vj);
+                s_i[k][r] = vi;
+                s_j[k][r] = vj;
             }
         }
-        __syncthreads();
+        // Chunk-uniform choice of the square: the integer-pipe one when every
+        // staged coordinate keeps all squares normal, else the hardware multiply.
+        const bool int_square = __syncthreads_and(safe);
         const int kend = min(KC, D - k0);
-        for (int k = 0; k < kend; ++k) {
-            Real xi[4], xj[4];
-            DistVec<Real>::load4(&s_i[k][ty * 4], xi);
-            DistVec<Real>::load4(&s_j[k][tx * 4], xj);
+        auto accumulate = [&](auto square) {
+            for (int k = 0; k < kend; ++k) {
+                Real xi[4], xj[4];
+                DistVec<Real>::load4(&s_i[k][ty * 4], xi);
+                DistVec<Real>::load4(&s_j[k][tx * 4], xj);
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+                for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const Real delta = T::sub(xi[a], xj[b]);
-                    acc[a][b] = T::add(acc[a][b], T::mul(delta, delta));
-                }
-        }
+                    for (int b = 0; b < 4; ++b) {
+                        const Real delta = T::sub(xi[a], xj[b]);
+                        acc[a][b] = T::add(acc[a][b], square(delta));
+                    }
+            }
+        };
+        if (sizeof(Real) == 8 && int_square) accumulate([](Real d) { return T::sqr(d); });
+        else accumulate([](Real d) { return T::mul(d, d); });
         __syncthreads();
     }
     int overflow = 0;

@@ -1,0 +1,189 @@
+// Exact IEEE-754 binary64 squaring on the integer pipes.
+//
+// GB300's FP64 pipe is a small fraction of its FP32/INT32 throughput, and the
+// float64 distance kernel (three FP64 operations per coordinate: subtract,
+// square, add) runs at that pipe's limit.  sqr_rn(d) returns the correctly
+// rounded (round-to-nearest-even) square of d computed with 32x32->64-bit
+// integer products, so the square moves to the integer pipes and only the
+// subtraction and the addition stay on the FP64 pipe.  The result is
+// bit-identical to d*d under IEEE-754 for every input: zero returns +0, and
+// values whose square is not a normal double (|d| < 2^-511 or |d| >= 2^511,
+// subnormals, infinities, NaN) take the hardware multiply behind a
+// warp-uniform branch, so no FP64 multiply is issued while every lane of the
+// warp is on the integer path.
+//
+// Method (the textbook integer multiply of two binary64 significands):
+//   d = m * 2^(e-1075), m = 2^52 | fraction (53 bits), e the biased exponent;
+//   m^2 = mh^2 * 2^64 + 2*mh*ml * 2^32 + ml^2 with mh the top 21 and ml the
+//   low 32 bits of m, so m^2 in [2^104, 2^106) is exact in 128 bits; it is
+//   normalised to have its top bit at 105, the top 53 bits are rounded to
+//   nearest-even on the remaining 53 bits, and the biased exponent of d^2 is
+//   2e - 1023 (+1 when m^2 >= 2^105); a rounding carry into bit 53 moves into
+//   the exponent field by the addition that packs the result.
+// Usable from host code (tests compare it with the host's multiply).
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define HDB_HD __host__ __device__ __forceinline__
+#else
+#define HDB_HD inline
+#endif
+
+namespace hdb {
+
+HDB_HD uint64_t exact_bits(double d) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t b;
+    std::memcpy(&b, &d, sizeof(b));
+    return b;
+#endif
+}
+
+HDB_HD double exact_double(uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+#endif
+}
+
+// 32-bit word primitives.  On GB300 64-bit integer adds, shifts and compares
+// are issued to the FP64 pipe, which is exactly the pipe being relieved, so
+// the square is written with 32-bit operations only.
+HDB_HD void mul_wide(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+#ifdef __CUDA_ARCH__
+    lo = a * b;
+    hi = __umulhi(a, b);
+#else
+    const uint64_t p = (uint64_t)a * (uint64_t)b;
+    lo = (uint32_t)p;
+    hi = (uint32_t)(p >> 32);
+#endif
+}
+
+// r = a + b + carry_in, carry_out in {0, 1}.
+HDB_HD uint32_t add_carry(uint32_t a, uint32_t b, uint32_t carry_in, uint32_t& carry_out) {
+    const uint32_t t = a + b;
+    const uint32_t c1 = t < a ? 1u : 0u;
+    const uint32_t r = t + carry_in;
+    carry_out = c1 | (r < t ? 1u : 0u);
+    return r;
+}
+
+// (hi:lo) >> s for 0 <= s < 32, low word.
+HDB_HD uint32_t funnel_right(uint32_t lo, uint32_t hi, uint32_t s) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_r(lo, hi, s);
+#else
+    return s ? (lo >> s) | (hi << (32 - s)) : lo;
+#endif
+}
+
+// (hi:lo) << s for 0 <= s < 32, high word.
+HDB_HD uint32_t funnel_left(uint32_t lo, uint32_t hi, uint32_t s) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(lo, hi, s);
+#else
+    return s ? (hi << s) | (lo >> (32 - s)) : hi;
+#endif
+}
+
+// Integer part of sqr_rn; valid for biased exponents 512..1533 (every normal
+// result) and for zero (returns +0), garbage elsewhere.  (hi, lo) are the two
+// words of d; every select stays on 32-bit words (a double-typed select is an
+// FP64-pipe instruction).
+HDB_HD double sqr_rn_words(uint32_t hi, uint32_t lo, bool zero) {
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    const uint32_t mh = (hi & 0xfffffu) | 0x100000u;  // top 21 bits of m
+    const uint32_t ml = lo;                           // low 32 bits of m
+    uint32_t p0h, p0l, p1h, p1l, p2h, p2l;
+    mul_wide(ml, ml, p0h, p0l);  // ml^2
+    mul_wide(mh, ml, p1h, p1l);  // mh*ml < 2^53
+    mul_wide(mh, mh, p2h, p2l);  // mh^2 < 2^42
+    // S = m^2 = p2 * 2^64 + p1 * 2^33 + p0 in words w3:w2:w1:w0.
+    uint32_t c1, c2, unused;
+    const uint32_t w0 = p0l;
+    const uint32_t w1 = add_carry(p0h, p1l << 1, 0u, c1);
+    const uint32_t w2 = add_carry(p2l, (p1h << 1) | (p1l >> 31), c1, c2);
+    const uint32_t w3 = add_carry(p2h, 0u, c2, unused);
+    const uint32_t top = (w3 >> 9) & 1u;  // S >= 2^105 (bit 105 = bit 9 of w3)
+    const uint32_t sh = 1u - top;         // normalise: top bit at 105
+    const uint32_t v3 = funnel_left(w2, w3, sh);
+    const uint32_t v2 = funnel_left(w1, w2, sh);
+    const uint32_t v1 = funnel_left(w0, w1, sh);
+    const uint32_t v0 = w0 << sh;
+    // Significand = S >> 53: bits 53..84 (low word) and 85..105 (high, hidden bit at 20).
+    uint32_t mlo = funnel_right(v1, v2, 21);
+    uint32_t mhi = funnel_right(v2, v3, 21) & 0x1fffffu;
+    // Remainder S mod 2^53: round bit = bit 52 (bit 20 of v1), sticky = bits 0..51.
+    const uint32_t round_bit = (v1 >> 20) & 1u;
+    const uint32_t sticky = (v1 & 0xfffffu) | v0;
+    const uint32_t up = round_bit & ((sticky != 0u ? 1u : 0u) | (mlo & 1u));
+    uint32_t carry;
+    mlo = add_carry(mlo, up, 0u, carry);
+    mhi += carry;
+    // Biased exponent E = 2e - 1023 + top; (E - 1) << 20 plus the high word
+    // (hidden bit included) packs it, a carry to 2^53 bumping the exponent.
+    const uint32_t rhi = zero ? 0u : ((2u * e - 1024u + top) << 20) + mhi;
+    mlo = zero ? 0u : mlo;
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)rhi, (int)mlo);
+#else
+    return exact_double(((uint64_t)rhi << 32) | mlo);
+#endif
+}
+
+// True when every difference a - b of two such values squares to a normal
+// double (or is zero): |a|, |b| in {0} U [2^-459, 2^509) give |RN(a - b)| = 0
+// or in [2^-511, 2^510], i.e. biased exponents 512..1533.
+HDB_HD bool sqr_operand_safe(double x) {
+#ifdef __CUDA_ARCH__
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+#else
+    const uint64_t bits = exact_bits(x);
+    const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
+#endif
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    return (((hi << 1) | lo) == 0u) || (e >= 1023u - 459u && e < 1023u + 509u);
+}
+
+// Square of a difference of sqr_operand_safe values (no hardware fallback).
+HDB_HD double sqr_rn_safe(double d) {
+#ifdef __CUDA_ARCH__
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+#else
+    const uint64_t bits = exact_bits(d);
+    const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
+#endif
+    return sqr_rn_words(hi, lo, ((hi << 1) | lo) == 0u);
+}
+
+HDB_HD double sqr_rn(double d) {
+#ifdef __CUDA_ARCH__
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+#else
+    const uint64_t bits = exact_bits(d);
+    const uint32_t hi = (uint32_t)(bits >> 32), lo = (uint32_t)bits;
+#endif
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    const bool zero = ((hi << 1) | lo) == 0u;
+    const bool hw = (e < 512u || e > 1533u) && !zero;  // square not a normal double
+    double r = sqr_rn_words(hi, lo, zero);
+#ifdef __CUDA_ARCH__
+    // Full-warp callers only: the branch is taken by the whole warp or not at all.
+    if (__any_sync(0xffffffffu, hw)) {
+        if (hw) r = __dmul_rn(d, d);
+    }
+#else
+    if (hw) r = d * d;
+#endif
+    return r;
+}
+
+}  // namespace hdb

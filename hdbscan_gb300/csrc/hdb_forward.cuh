@@ -312,7 +312,7 @@ __device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char*
             static_cast<Real*>(args.edge_w)[ebase + i] = a.r0[i];
         }
     }
-    sort_edges_warp<Real>(a, m);
+    sort_edges_warp<Real>(a, m, args.unit_core != 0);
     if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
     if (args.order)
         for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
@@ -364,8 +364,11 @@ struct WindowMeta {
 
 // Dynamic shared memory: n_arenas arenas of arena_stride bytes, then the
 // staged window (x_off) and its core distances (core_off); see the plan layer.
-template <typename Real, int PT, int SV, int DP>
-__global__ void __launch_bounds__(PT + 32, 1) hdb_forward_kernel(const __grid_constant__ ForwardArgs args) {
+// MINB CTAs share an SM (register budget from the launch bounds): with two,
+// one window's barrier and reduction latency hides behind another's distance
+// arithmetic.
+template <typename Real, int PT, int SV, int DP, int MINB>
+__global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid_constant__ ForwardArgs args) {
     using T = RealTraits<Real>;
     using Key = typename T::Bits;
     constexpr int PW = PT / 32;

@@ -10,22 +10,23 @@
 namespace hdb {
 
 template <typename Real>
-bool forward_layout(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out);
+bool forward_layout(int n, int dp, bool unit_core, size_t budget, int max_arenas, ForwardLayout* out);
 
-template <typename Real, int THREADS, int V, int DP>
+template <typename Real, int THREADS, int V, int DP, int MINB>
 cudaError_t launch_forward(const ForwardArgs& a, int grid, size_t smem, cudaStream_t s, int priority) {
-    return launch_ex(hdb_forward_kernel<Real, THREADS, V, DP>, grid, THREADS + 32, smem, s, priority, 1, a);
+    return launch_ex(hdb_forward_kernel<Real, THREADS, V, DP, MINB>, grid, THREADS + 32, smem, s, priority, 1, a);
 }
 
-template <typename Real, int DP>
+// Several CTAs per SM keep one arena each: the other CTAs provide the overlap.
+template <typename Real, int DP, int MINB>
 bool single_layout(int n, bool unit_core, size_t budget, ForwardLayout* out) {
-    return forward_layout<Real>(n, DP, unit_core, budget, out);
+    return forward_layout<Real>(n, DP, unit_core, budget, MINB > 1 ? 1 : 2, out);
 }
 
-template <typename Real, int THREADS, int V, int DP>
+template <typename Real, int THREADS, int V, int DP, int MINB = 1>
 constexpr ForwardVariant forward_variant() {
-    return ForwardVariant{THREADS, V, DP, 1, (const void*)hdb_forward_kernel<Real, THREADS, V, DP>,
-                          launch_forward<Real, THREADS, V, DP>, single_layout<Real, DP>};
+    return ForwardVariant{THREADS, V, DP, 1, MINB, (const void*)hdb_forward_kernel<Real, THREADS, V, DP, MINB>,
+                          launch_forward<Real, THREADS, V, DP, MINB>, single_layout<Real, DP, MINB>};
 }
 
 template <typename Real, int K, int DP>
@@ -66,13 +67,14 @@ cudaError_t launch_backward(const BackwardArgs& a, int grid, cudaStream_t s, int
 // Two arenas (Prim/tree overlap) when they fit next to the staged window,
 // else one arena with the staged window, else one arena alone.
 template <typename Real>
-bool forward_layout(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out) {
+bool forward_layout(int n, int dp, bool unit_core, size_t budget, int max_arenas, ForwardLayout* out) {
     const size_t arena = (Arena<Real>::bytes(n) + 127) & ~size_t(127);
     const size_t x = dp > 0 ? (((size_t)n * dp * sizeof(Real) + 127) & ~size_t(127)) : 0;
     const size_t core = unit_core ? 0 : (((size_t)Arena<Real>::round_cap(n) * sizeof(Real) + 127) & ~size_t(127));
     const int nbs[3] = {2, 1, 1};
     const int xss[3] = {1, 1, 0};
     for (int c = 0; c < 3; ++c) {
+        if (nbs[c] > max_arenas) continue;
         const int xs = dp > 0 ? xss[c] : 0;
         const size_t bytes = nbs[c] * arena + (xs ? x : 0) + core;
         if (bytes <= budget) {

@@ -30,6 +30,12 @@ const ForwardVariant kForward[] = {
     forward_variant<float, 512, 4, 0>(),
     forward_variant<float, 512, 8, 8>(),
     forward_variant<float, 512, 8, 0>(),
+    // Two CTAs per SM.
+    forward_variant<float, 256, 4, 8, 2>(),
+    forward_variant<float, 256, 4, 16, 2>(),
+    forward_variant<float, 128, 4, 8, 2>(),
+    forward_variant<float, 128, 4, 16, 2>(),
+    forward_variant<float, 128, 4, 32, 2>(),
 };
 const CoreVariant kCore[] = {
     core_points_variant<float, 8, 8>(),   core_points_variant<float, 8, 16>(),

@@ -105,7 +105,9 @@ const hdb::ForwardVariant* pick_forward(const hdb::PrecisionKernels& k, int prec
     for (int dp : {8, 16, 32}) {
         if (dims > dp || v * dp * words > 64) continue;
         for (int i = 0; i < k.n_forward; ++i)
-            if (k.forward[i].threads == threads && k.forward[i].v == v && k.forward[i].dp == dp) return &k.forward[i];
+            if (k.forward[i].threads == threads && k.forward[i].v == v && k.forward[i].dp == dp &&
+                k.forward[i].per_sm == 1)
+                return &k.forward[i];
     }
     return nullptr;
 }
@@ -171,7 +173,7 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     if (e != cudaSuccess) return fail(HDB_E_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
     const size_t budget = (size_t)optin > attr.sharedSizeBytes + 1024 ? (size_t)optin - attr.sharedSizeBytes - 1024 : 0;
     hdb::ForwardLayout layout{};
-    if (!k.forward_layout(n, fv->dp, unit, budget, &layout))
+    if (!k.forward_layout(n, fv->dp, unit, budget, 2, &layout))
         return fail(HDB_E_INVALID, "window exceeds shared memory");
     const size_t smem = layout.bytes;
     e = hdb::raise_dynamic_smem(fv->func, smem);

@@ -25,6 +25,7 @@ struct ForwardVariant {
     int v;        // vertices (slots) per Prim thread
     int dp;       // padded register dimensions; 0 = matrix variant
     int cluster;  // CTAs per window (1 = hdb_forward_kernel, else a cluster of hdb_cluster_forward_kernel)
+    int per_sm;   // CTAs per SM the variant is built for (launch bounds, shared-memory budget)
     const void* func;
     cudaError_t (*launch)(const ForwardArgs&, int grid, size_t smem, cudaStream_t, int priority);
     // Shared-memory layout for windows of up to n points within `budget` bytes; false if none fits.
@@ -50,8 +51,9 @@ struct PrecisionKernels {
     cudaError_t (*launch_select)(const CoreArgs&, int grid, size_t smem, cudaStream_t, int priority);
     const void* select_func;
     cudaError_t (*launch_backward)(const BackwardArgs&, int grid, cudaStream_t, int priority);
-    // Best single-CTA layout for windows of up to n points within `budget` bytes; false if none fits.
-    bool (*forward_layout)(int n, int dp, bool unit_core, size_t budget, ForwardLayout* out);
+    // Best single-CTA layout (at most max_arenas arenas) for windows of up to n
+    // points within `budget` bytes; false if none fits.
+    bool (*forward_layout)(int n, int dp, bool unit_core, size_t budget, int max_arenas, ForwardLayout* out);
 };
 
 const PrecisionKernels& kernels_f32();

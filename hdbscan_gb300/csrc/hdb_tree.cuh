@@ -17,9 +17,20 @@
 //    the segment plus K/32 swap rounds, with NumPy's exact swap sequence.
 //    Segments of <= 16 elements and depth-exhausted heapsort segments are
 //    finished one per lane.
+//  * windows whose edge weights are all distinct are sorted by a stable warp
+//    LSD radix sort instead (the argsort of distinct keys is unique, so it
+//    equals NumPy's); a window with any tied weight falls back to the exact
+//    introsort above;
 //  * linkage uses union by size over packed 64-bit words
 //    (parent | component node << 16 | size << 32) without path compression;
 //    the roots, hence the tree, are those of the reference's union-find.
+//  * condensation runs the reference's breadth-first queue one level at a
+//    time across the warp: every cluster is a path of the dendrogram (it only
+//    branches where it ends in a split), so the nodes of one level belong to
+//    distinct clusters and each lane's stability sum keeps the reference's
+//    addition order; split children take consecutive ids by a ballot prefix
+//    over the level, i.e. in queue order.  Pruned points find their cluster
+//    afterwards from their lowest large ancestor.
 //  * selection uses the binary shape of the condensed tree (every split
 //    creates exactly two consecutive ids), as the reference's
 //    COOPERATIVE_BINARY_EOM variant does (_kernels.py:648-669).
@@ -188,11 +199,89 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
     return i;
 }
 
-// Sorts r0[0..m) with NumPy's quicksort order; leaves the order in s2 and the
-// sorted weights in r0.  Whole-warp call.
+// Stable LSD radix sort (8-bit digits) of the order-preserving keys of
+// r0[0..m) with their indices, by one warp.  Returns false, leaving r0 intact,
+// when two keys are equal; otherwise writes the order to s2 and the sorted
+// weights to r0.  Needs m >= 256 (the digit histogram lives in s5..s6).
 template <typename Real>
-__device__ void sort_edges_warp(const Arena<Real>& a, int m) {
+__device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
+    using T = RealTraits<Real>;
+    using Key = typename T::Bits;
+    constexpr int kPasses = (int)sizeof(Key);
     const int lane = threadIdx.x & 31;
+    const unsigned lt = lanemask_lt();
+    Key* kin = reinterpret_cast<Key*>(a.r1);
+    Key* kout = reinterpret_cast<Key*>(a.r2);
+    int16_t* iin = a.s3;
+    int16_t* iout = a.s4;
+    int* hist = reinterpret_cast<int*>(a.s5);
+    for (int i = lane; i < m; i += 32) { kin[i] = T::key(a.r0[i]); iin[i] = (int16_t)i; }
+    __syncwarp();
+    for (int pass = 0; pass < kPasses; ++pass) {
+        const int shift = 8 * pass;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) hist[8 * lane + b] = 0;
+        __syncwarp();
+        for (int base = 0; base < m; base += 32) {
+            const int i = base + lane;
+            const int d = i < m ? (int)((kin[i] >> shift) & 0xff) : 256;
+            const unsigned same = __match_any_sync(0xffffffffu, d);
+            if (d < 256 && (same & lt) == 0) hist[d] += __popc(same);
+            __syncwarp();
+        }
+        // Exclusive scan; each lane owns 8 consecutive digits.
+        int local[8], sum = 0, full = 0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) { local[b] = hist[8 * lane + b]; full |= local[b] == m; sum += local[b]; }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (__any_sync(0xffffffffu, full)) continue;  // one digit holds every key: this pass keeps the order
+        int run = incl - sum;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) { hist[8 * lane + b] = run; run += local[b]; }
+        __syncwarp();
+        for (int base = 0; base < m; base += 32) {
+            const int i = base + lane;
+            const bool valid = i < m;
+            const Key k = valid ? kin[i] : Key(0);
+            const int d = valid ? (int)((k >> shift) & 0xff) : 256;
+            const unsigned same = __match_any_sync(0xffffffffu, d);
+            int pos = 0;
+            if (valid) pos = hist[d] + __popc(same & lt);
+            __syncwarp();
+            if (valid) {
+                kout[pos] = k;
+                iout[pos] = iin[i];
+                if ((same & lt) == 0) hist[d] += __popc(same);
+            }
+            __syncwarp();
+        }
+        Key* kt = kin; kin = kout; kout = kt;
+        int16_t* it = iin; iin = iout; iout = it;
+        __syncwarp();
+    }
+    bool dup = false;
+    for (int i = lane; i + 1 < m; i += 32) dup |= kin[i] == kin[i + 1];
+    if (__any_sync(0xffffffffu, dup)) return false;
+    for (int i = lane; i < m; i += 32) {
+        a.s2[i] = iin[i];
+        a.r0[i] = T::from_key(kin[i]);
+    }
+    __syncwarp();
+    return true;
+}
+
+// Sorts r0[0..m) with NumPy's quicksort order; leaves the order in s2 and the
+// sorted weights in r0.  Whole-warp call.  try_radix: attempt the tie-free
+// radix path first (worth it where ties are rare: min_samples <= 2).
+template <typename Real>
+__device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
+    const int lane = threadIdx.x & 31;
+    if (try_radix && m >= 256 && radix_sort_distinct_warp<Real>(a, m)) return;
     SortPair<Real>* p = reinterpret_cast<SortPair<Real>*>(a.r1);
     for (int i = lane; i < m; i += 32) { p[i].w = a.r0[i]; p[i].idx = i; }
     int16_t *task_lo = a.s5, *task_hi = a.s6, *task_depth = a.s7;  // depth*2 + checked
@@ -262,8 +351,10 @@ __device__ void linkage_warp(const Arena<Real>& a, int n) {
         U[x] = (unsigned long long)x | ((unsigned long long)x << 16) | (1ull << 32);
     __syncwarp();
     if (lane == 0) {
+        int xn = a.s2[0], yn = a.s3[0];  // n >= 2: at least one edge
         for (int i = 0; i < n - 1; ++i) {
-            int x = a.s2[i], y = a.s3[i];
+            int x = xn, y = yn;
+            if (i + 2 < n) { xn = a.s2[i + 1]; yn = a.s3[i + 1]; }  // next endpoints, off the critical path
             unsigned long long wx = U[x], wy = U[y];
             while ((int)(wx & 0xffff) != x) { x = (int)(wx & 0xffff); wx = U[x]; }
             while ((int)(wy & 0xffff) != y) { y = (int)(wy & 0xffff); wy = U[y]; }
@@ -285,93 +376,111 @@ __device__ void linkage_warp(const Arena<Real>& a, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// Breadth-first condensation (reference: _kernels.py:558-643).  Lane 0 runs
-// the queue; lanes initialise.  Linkage node ids n..2n-2 (index id-n); cluster
-// ids n.. (index id-n).  Returns next_label (warp-uniform).
+// Breadth-first condensation (reference: _kernels.py:558-643), one queue
+// level per warp round.  Linkage node ids n..2n-2 (index id-n); cluster ids
+// n.. (index id-n).  Inputs: s4 left, s5 right, s6 size, r0 merge weights
+// (turned into lambda = 1/weight in place).  Outputs: s2 cluster parent, r1
+// birth, r2 stability, sel, s9 point parent.  Returns next_label
+// (warp-uniform).
 // ---------------------------------------------------------------------------
 template <typename Real>
 __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
+    using T = RealTraits<Real>;
     const int lane = threadIdx.x & 31;
-    int16_t* relabel = a.s7;
-    int16_t* queue = a.s8;
-    int16_t* prune = a.s0;   // 2*cap entries across s0,s1
+    const unsigned lt = lanemask_lt();
+    int16_t* relabel = a.s7;   // cluster of each large linkage node
+    int16_t* queue = a.s8;     // large linkage nodes in breadth-first order
+    int16_t* dparent = a.s0;   // dendrogram parent of node ids 0..2n-3 (spans s0, s1)
     int16_t* parent = a.s2;
     Real* birth = a.r1;
     Real* stab = a.r2;
+    Real* lam = a.r0;
     const int16_t* left = a.s4;
     const int16_t* right = a.s5;
     const int16_t* size = a.s6;
-    const Real inf = RealTraits<Real>::inf();
+    const Real inf = T::inf();
     for (int c = lane; c < n; c += 32) { parent[c] = -1; birth[c] = 0; stab[c] = 0; a.sel[c] = 0; }
+    for (int i = lane; i < n - 1; i += 32) {
+        const Real d = lam[i];
+        lam[i] = d > Real(0) ? T::recip(d) : inf;
+        dparent[left[i]] = (int16_t)(n + i);
+        dparent[right[i]] = (int16_t)(n + i);
+    }
+    const int root = 2 * n - 2;
+    if (lane == 0) { queue[0] = (int16_t)root; relabel[root - n] = (int16_t)n; }
     __syncwarp();
-    int next_label = n + 1;
-    if (lane == 0) {
-        const int root = 2 * n - 2;
-        int head = 0, tail = 1;
-        queue[0] = (int16_t)root;
-        relabel[root - n] = (int16_t)n;
-        while (head < tail) {
-            const int node = queue[head++];
-            const int ni = node - n;
-            const int l = left[ni], r = right[ni];
-            const int cluster = relabel[ni];
-            const int ci = cluster - n;
-            const Real cluster_birth = birth[ci];
-            Real cluster_stability = stab[ci];
-            const Real dist = a.r0[ni];
-            const Real lambda = dist > Real(0) ? RealTraits<Real>::recip(dist) : inf;
-            const int size_l = l < n ? 1 : size[l - n];
-            const int size_r = r < n ? 1 : size[r - n];
-            const bool large_l = size_l >= mcs, large_r = size_r >= mcs;
-            if (large_l && large_r) {
-                // Both children: new consecutive ids (_kernels.py:603-613).
-                for (int k = 0; k < 2; ++k) {
-                    const int child = k == 0 ? l : r;
-                    const int csize = k == 0 ? size_l : size_r;
-                    const int label = next_label++;
-                    relabel[child - n] = (int16_t)label;
-                    parent[label - n] = (int16_t)cluster;
-                    birth[label - n] = lambda;
-                    a.sel[label - n] = 1;
-                    cluster_stability = RealTraits<Real>::add(
-                        cluster_stability,
-                        RealTraits<Real>::mul(RealTraits<Real>::sub(lambda, cluster_birth), (Real)csize));
-                    queue[tail++] = (int16_t)child;
-                }
-            } else {
-                for (int k = 0; k < 2; ++k) {
-                    const int child = k == 0 ? l : r;
-                    if (k == 0 ? large_l : large_r) {
-                        relabel[child - n] = (int16_t)cluster;
-                        queue[tail++] = (int16_t)child;
-                    } else {
-                        // Prune the whole subtree leaf by leaf (_kernels.py:626-637);
-                        // every leaf adds the same term, so only the count matters.
-                        const Real term = RealTraits<Real>::sub(lambda, cluster_birth);
-                        if (child < n) {
-                            a.s9[child] = (int16_t)cluster;
-                            cluster_stability = RealTraits<Real>::add(cluster_stability, term);
+    int head = 0, tail = 1, next_label = n + 1;
+    while (head < tail) {  // tail <= n - 1 (every node is queued at most once)
+        const int level_end = tail;
+        for (int base = head; base < level_end; base += 32) {
+            const int q = base + lane;
+            const bool valid = q < level_end;
+            int l = 0, r = 0, cluster = n, size_l = 0, size_r = 0;
+            Real lambda = Real(0);
+            if (valid) {
+                const int ni = queue[q] - n;
+                l = left[ni];
+                r = right[ni];
+                cluster = relabel[ni];
+                lambda = lam[ni];
+                size_l = l < n ? 1 : size[l - n];
+                size_r = r < n ? 1 : size[r - n];
+            }
+            const bool large_l = valid && size_l >= mcs, large_r = valid && size_r >= mcs;
+            const bool split = large_l && large_r;
+            const unsigned b1 = __ballot_sync(0xffffffffu, large_l || large_r);
+            const unsigned b2 = __ballot_sync(0xffffffffu, split);
+            const int pos = tail + __popc(b1 & lt) + __popc(b2 & lt);
+            const int label0 = next_label + 2 * __popc(b2 & lt);
+            if (valid) {
+                const int ci = cluster - n;
+                const Real cb = birth[ci];
+                Real st = stab[ci];
+                if (split) {
+                    // Both children: new consecutive ids (_kernels.py:603-613).
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const int child = k == 0 ? l : r;
+                        const int csize = k == 0 ? size_l : size_r;
+                        const int label = label0 + k;
+                        relabel[child - n] = (int16_t)label;
+                        parent[label - n] = (int16_t)cluster;
+                        birth[label - n] = lambda;
+                        a.sel[label - n] = 1;
+                        st = T::add(st, T::mul(T::sub(lambda, cb), (Real)csize));
+                        queue[pos + k] = (int16_t)child;
+                    }
+                } else {
+                    // A large child continues the cluster; a small one is
+                    // pruned leaf by leaf, each leaf adding the same term
+                    // (_kernels.py:614-637).
+                    const Real term = T::sub(lambda, cb);
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        const int child = k == 0 ? l : r;
+                        if (k == 0 ? large_l : large_r) {
+                            relabel[child - n] = (int16_t)cluster;
+                            queue[pos] = (int16_t)child;
                         } else {
-                            int ph = 0, pt = 0, leaf = child;
-                            for (;;) {
-                                if (leaf < n) {
-                                    a.s9[leaf] = (int16_t)cluster;
-                                    cluster_stability = RealTraits<Real>::add(cluster_stability, term);
-                                } else {
-                                    prune[pt++] = left[leaf - n];
-                                    prune[pt++] = right[leaf - n];
-                                }
-                                if (ph == pt) break;
-                                leaf = prune[ph++];
-                            }
+                            const int csize = k == 0 ? size_l : size_r;
+                            for (int t = 0; t < csize; ++t) st = T::add(st, term);
                         }
                     }
                 }
+                stab[ci] = st;
             }
-            stab[ci] = cluster_stability;
+            tail += __popc(b1) + __popc(b2);
+            next_label += 2 * __popc(b2);
         }
+        __syncwarp();
+        head = level_end;
     }
-    next_label = __shfl_sync(0xffffffffu, next_label, 0);
+    // Every point was pruned at its lowest large ancestor (or the root).
+    for (int i = lane; i < n; i += 32) {
+        int v = dparent[i];
+        while (v != root && size[v - n] < mcs) v = dparent[v];
+        a.s9[i] = relabel[v - n];
+    }
     __syncwarp();
     return next_label;
 }
@@ -396,6 +505,7 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
     for (int child = n + 1 + 2 * lane; child < next_label; child += 64) first[parent[child - n] - n] = (int16_t)child;
     __syncwarp();
     if (lane == 0) {
+        // 1. Excess of mass, children (larger ids) before parents.
         for (int node = next_label - 1; node > n; --node) {
             const int f = first[node - n];
             const Real subtree = f < 0 ? Real(0)
@@ -406,36 +516,43 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
                 stab[node - n] = subtree;
             }
         }
-        // Parents have smaller ids: one forward pass suppresses descendants.
+        // 2. Parents first (ascending ids): suppress the descendants of a
+        //    selected cluster; with epsilon, mark the cluster each surviving
+        //    selection resolves to (itself, or its epsilon stop ancestor).
         int16_t* blocked = a.s4;
-        blocked[0] = 0;
-        for (int node = n + 1; node < next_label; ++node) {
-            const int inherited = blocked[parent[node - n] - n];
-            blocked[node - n] = (int16_t)(inherited || a.sel[node - n]);
-            if (inherited) a.sel[node - n] = 0;
-        }
+        int16_t* stop = a.s5;
         int16_t* label_map = a.s6;
-        for (int c = 0; c < clusters; ++c) label_map[c] = -1;
-        if (epsilon > Real(0)) {
-            int16_t* stop = a.s5;
-            for (int node = n + 1; node < next_label; ++node) {
-                const int anc = parent[node - n];
-                stop[node - n] = (int16_t)(anc == n ? node
-                                                    : (RealTraits<Real>::recip(birth[anc - n]) > epsilon ? anc
-                                                                                                         : stop[anc - n]));
-                if (!a.sel[node - n]) continue;
-                const int chosen = RealTraits<Real>::recip(birth[node - n]) < epsilon ? stop[node - n] : node;
-                label_map[chosen - n] = 1;
+        blocked[0] = 0;
+        label_map[0] = -1;
+        for (int node = n + 1; node < next_label; ++node) {
+            const int anc = parent[node - n];
+            const int inherited = blocked[anc - n];
+            int selected = a.sel[node - n];
+            blocked[node - n] = (int16_t)(inherited || selected);
+            if (inherited) selected = 0;
+            a.sel[node - n] = (uint8_t)selected;
+            label_map[node - n] = -1;
+            if (epsilon > Real(0)) {
+                const int st = anc == n ? node
+                                        : (RealTraits<Real>::recip(birth[anc - n]) > epsilon ? anc : stop[anc - n]);
+                stop[node - n] = (int16_t)st;
+                if (selected) {
+                    const int chosen = RealTraits<Real>::recip(birth[node - n]) < epsilon ? st : node;
+                    label_map[chosen - n] = 1;
+                }
             }
-            for (int node = n + 1; node < next_label; ++node) a.sel[node - n] = label_map[node - n] == 1;
         }
-        int label = 0;
-        for (int node = n + 1; node < next_label; ++node)
-            if (a.sel[node - n]) label_map[node - n] = (int16_t)label++;
+        // 3. Ascending: final selection, label numbers, label of every cluster.
         int16_t* resolved = a.s7;
         resolved[0] = -1;
-        for (int node = n + 1; node < next_label; ++node)
-            resolved[node - n] = a.sel[node - n] ? label_map[node - n] : resolved[parent[node - n] - n];
+        int label = 0;
+        for (int node = n + 1; node < next_label; ++node) {
+            const int selected = epsilon > Real(0) ? (label_map[node - n] == 1) : a.sel[node - n];
+            a.sel[node - n] = (uint8_t)selected;
+            const int lm = selected ? label++ : -1;
+            label_map[node - n] = (int16_t)lm;
+            resolved[node - n] = (int16_t)(selected ? lm : resolved[parent[node - n] - n]);
+        }
     }
     __syncwarp();
     for (int i = lane; i < n; i += 32) labels[i] = a.s7[a.s9[i] - n];

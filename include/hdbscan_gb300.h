@@ -91,11 +91,12 @@ int hdb_version(void);
 const char* hdb_last_error(void);
 
 /* Autotune table used by later hdb_plan_create calls (process-wide).  Each
- * rule is 8 int32: {precision (HDB_F32/HDB_F64/-1 any), unit core (1 =
+ * rule is 9 int32: {precision (HDB_F32/HDB_F64/-1 any), unit core (1 =
  * min_samples <= 2, 0 = core distances, -1 any), n_max, d_max, Prim threads,
  * slots per thread, register dims (0 = matrix variant), CTAs per window (1 =
- * one CTA, 2..8 = a thread-block cluster)}; the first rule that matches a
- * window and names a compiled variant wins, built-in defaults back it up.
+ * one CTA, 2..8 = a thread-block cluster), CTAs per SM (1..4)}; the first rule
+ * that matches a window and names a compiled variant wins, built-in defaults
+ * back it up.
  * n_rules = 0 restores the defaults.  Replaces the fixed launch choice of
  * hdbscan_gpu/_cuda.py:82-88 (block width, register Prim, shared arena). */
 int hdb_set_tuning(const int32_t* rules, int n_rules);
@@ -104,8 +105,8 @@ int hdb_set_tuning(const int32_t* rules, int n_rules);
 int hdb_get_tuning(int32_t* rules, int capacity);
 
 /* Compiled forward variants of a precision as {Prim threads, slots, register
- * dims (0 = matrix), CTAs per window} quadruples; returns their count (the
- * autotuner's candidates). */
+ * dims (0 = matrix), CTAs per window, CTAs per SM} 5-tuples; returns their
+ * count (the autotuner's candidates). */
 int hdb_list_variants(int precision, int32_t* out, int capacity);
 
 /* Build a plan for a ragged batch: `windows` windows whose points are rows

@@ -50,8 +50,8 @@ class forced_variant:
         from hdbscan_gb300 import _lib
 
         code = _lib.HDB_F32 if precision == "float32" else _lib.HDB_F64
-        rules = [] if small else [[code, -1, 1024, 1 << 20, 512, 2, 0, 1]]
-        rules.append([code, -1, 4096, 1 << 20, threads, slots, dims, cluster])
+        rules = [] if small else [[code, -1, 1024, 1 << 20, 512, 2, 0, 1, 1]]
+        rules.append([code, -1, 4096, 1 << 20, threads, slots, dims, cluster, 1])
         self.rules = np.array(rules, dtype=np.int32)
 
     def __enter__(self):
