@@ -407,7 +407,8 @@ def main():
     traffic_path = ROOT / "profiles" / f"traffic_{args.config}.json"
     if traffic_path.exists():
         traffic = json.loads(traffic_path.read_text()).get("dram_bytes_per_launch")
-    launches_per_step = len(describe["classes"]) + len(describe["core"]) + (1 if describe["distance_tiles"] else 0)
+    launches_per_step = (len(describe["classes"]) + len(describe["core"]) +
+                         sum(1 for c in describe["classes"] if c["distance_tiles"]))
     if backward:
         launches_per_step += 2  # dX zeroing + backward kernel
     line = {

@@ -341,7 +341,7 @@ int build_plan(hdb_plan* p) {
             for (int w : c.windows) {
                 const int n = size_of(w);
                 if (launch.cv) {
-                    for (int r = 0; r < n; r += 128) { launch.items.push_back(w); launch.items.push_back(r); }
+                    for (int r = 0; r < n; r += launch.cv->rows) { launch.items.push_back(w); launch.items.push_back(r); }
                 } else {
                     for (int r = 0; r < n; ++r) { select.items.push_back(w); select.items.push_back(r); }
                 }
@@ -749,6 +749,7 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
              ",\"per_sm\":" + std::to_string(c.fv->per_sm) +
              ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
              "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
+             ",\"distance_tiles\":" + std::to_string(c.n_tiles) + ",\"priority\":" + std::to_string(c.priority) +
              ",\"windows\":" +
              std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
              std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";

@@ -153,7 +153,8 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
 // Core distances.
 // ---------------------------------------------------------------------------
 
-constexpr int kCoreRows = 128;
+constexpr int kCoreRows = 128;        // rows per CTA of the points kernel
+constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel: many CTAs keep loads in flight
 constexpr int kCorePrefetch = 16;
 
 // Insert (d, j) into the ascending register list L/LI of length K; strict '<'
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
 // Rows from the materialized matrix: thread i reads column i (the block is
 // symmetric), so every step is one coalesced row segment.
 template <typename Real, int K>
-__global__ void __launch_bounds__(kCoreRows) hdb_core_matrix_kernel(const CoreArgs args) {
+__global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_kernel(const CoreArgs args) {
     using T = RealTraits<Real>;
     const int item = blockIdx.x;
     if (item >= args.n_items) return;

@@ -36,17 +36,17 @@ cudaError_t launch_core_points(const CoreArgs& a, int grid, cudaStream_t s, int 
 
 template <typename Real, int K>
 cudaError_t launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
-    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreRows, 0, s, priority, 1, a);
+    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows, 0, s, priority, 1, a);
 }
 
 template <typename Real, int K, int DP>
 constexpr CoreVariant core_points_variant() {
-    return CoreVariant{K, DP, (const void*)hdb_core_points_kernel<Real, K, DP>, launch_core_points<Real, K, DP>};
+    return CoreVariant{K, DP, kCoreRows, (const void*)hdb_core_points_kernel<Real, K, DP>, launch_core_points<Real, K, DP>};
 }
 
 template <typename Real, int K>
 constexpr CoreVariant core_matrix_variant() {
-    return CoreVariant{K, 0, (const void*)hdb_core_matrix_kernel<Real, K>, launch_core_matrix<Real, K>};
+    return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_kernel<Real, K>, launch_core_matrix<Real, K>};
 }
 
 template <typename Real>

@@ -193,7 +193,7 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     int32_t* ticket = reinterpret_cast<int32_t*>(scratch + kOffTicket);
     int32_t* items = reinterpret_cast<int32_t*>(scratch + kOffItems);
     void* core = scratch + kOffCore;
-    const int rows_per_item = unit ? 1 : (cv ? 128 : 1);
+    const int rows_per_item = unit ? 1 : (cv ? cv->rows : 1);
     const int n_items = unit ? 0 : batch * ((n + rows_per_item - 1) / rows_per_item);
     const int work = (batch + 1 > n_items ? batch + 1 : n_items);
     noalloc_tables_kernel<<<(work + 255) / 256, 256, 0, stream>>>(offsets, queue, ticket, items, batch, n,

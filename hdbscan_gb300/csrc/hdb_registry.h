@@ -35,6 +35,7 @@ struct ForwardVariant {
 struct CoreVariant {
     int k;        // list length (max ms)
     int dp;       // padded register dimensions; 0 = matrix variant
+    int rows;     // rows per CTA (work items start every `rows` rows)
     const void* func;
     cudaError_t (*launch)(const CoreArgs&, int grid, cudaStream_t, int priority);
 };
