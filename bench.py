@@ -170,6 +170,40 @@ def run_reference_arm(args, packed, offsets, params):
     print(json.dumps(line))
 
 
+def dist_env():
+    """(rank, world, local rank) from the torchrun environment (1 process = 1 GPU)."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def rank_workload(config, rank, windows=None):
+    """This rank's shard of a weak-scaling run: the config's batch drawn with the seed of shard `rank`
+    (rank 0 is the config itself).  Windows are independent, so ranks exchange no data."""
+    from hdbscan_gb300 import synthetic
+
+    kwargs = {"windows": windows} if windows else {}
+    if rank:
+        kwargs["seed"] = synthetic.SEEDS[config] + 7919 * rank
+    return synthetic.make(config, **kwargs)
+
+
+def reduce_max(value, world, device):
+    """Max over ranks (the slowest rank bounds the whole job)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(windows_per_rank, world, ms_per_step):
+    """Units all ranks processed per second of the max-over-ranks step time."""
+    return windows_per_rank * world / (ms_per_step / 1e3)
+
+
 def main():
     parser = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     parser.add_argument("--gpus", type=int, default=1)
@@ -191,11 +225,8 @@ def main():
     if args.warmup < 3:
         parser.error("--warmup must be >= 3")
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    from hdbscan_gb300 import synthetic
-
-    packed64, offsets, params = synthetic.make(args.config, **({"windows": args.windows} if args.windows else {}))
+    rank, world, local = dist_env()
+    packed64, offsets, params = rank_workload(args.config, rank, args.windows)
     if args.impl == "reference":
         if rank == 0:
             run_reference_arm(args, packed64, offsets, params)
@@ -207,7 +238,6 @@ def main():
     from hdbscan_gb300 import _lib
     from hdbscan_gb300._cuda import Plan, raise_for_status
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     if world > 1:
@@ -268,12 +298,8 @@ def main():
     if args.profile:
         print(json.dumps({"profile_ms_per_step": float(np.mean(step_ms))}))
         return
-    ms_per_step = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms_per_step], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_per_step = float(t.item())
-    value = B * world / (ms_per_step / 1e3)
+    ms_per_step = reduce_max(float(np.mean(step_ms)), world, device)
+    value = whole_job_rate(B, world, ms_per_step)
 
     # ---- kernel-only timing of the forward kernel (non-graph launch) --------
     kernel_ms = []
@@ -339,7 +365,7 @@ def main():
         end.record(stream)
         end.synchronize()
         plain_ms.append(start.elapsed_time(end))
-    plain_value = B / (float(np.mean(plain_ms)) / 1e3)
+    plain_value = whole_job_rate(B, world, reduce_max(float(np.mean(plain_ms)), world, device))
     plain_exact = bool(np.array_equal(plain_labels.cpu().numpy(), graph_labels))
 
     # ---- end to end through the public API ----------------------------------
@@ -369,7 +395,7 @@ def main():
         if step >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_exact = bool(np.array_equal(out.numpy().reshape(-1), graph_labels))
-    e2e_value = B / (float(np.median(e2e_ms)) / 1e3)
+    e2e_value = whole_job_rate(B, world, reduce_max(float(np.median(e2e_ms)), world, device))
 
     # ---- oracle parity on a sample + CPU baseline ---------------------------
     from oracle import oracle
