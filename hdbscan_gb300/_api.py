@@ -43,6 +43,15 @@ def _torch_bool():
     return torch.bool
 
 
+def validate_selection(cluster_selection_method, allow_single_cluster):
+    """Checks of the selection options beyond the reference's fixed contract."""
+    if cluster_selection_method not in ("eom", "leaf"):
+        raise ValueError("cluster_selection_method must be 'eom' or 'leaf'")
+    if not isinstance(allow_single_cluster, (bool, np.bool_)):
+        raise ValueError("allow_single_cluster must be a bool")
+    return cluster_selection_method, bool(allow_single_cluster)
+
+
 def validate_parameters(min_cluster_size, min_samples, cluster_selection_epsilon, backend, precision):
     """Parameter checks of hdbscan_gpu/_api.py:32-56; returns (mcs, ms, eps)."""
     if backend not in ("mlx", "cuda"):
@@ -93,6 +102,9 @@ def hdbscan(
     cluster_selection_epsilon=0.0,
     backend="cuda",
     precision="float32",
+    cluster_selection_method="eom",
+    allow_single_cluster=False,
+    return_probabilities=False,
 ):
     """Return device labels for Euclidean EOM HDBSCAN, excluding the root.
 
@@ -104,9 +116,16 @@ def hdbscan(
     produced on the caller's current stream.  Windows hold at most 4096
     points.  Float32 rounding can change near-tied hierarchies relative to
     scikit-learn's float64 calculation, exactly as in the reference.
+
+    Beyond the reference's fixed contract (its defaults): cluster_selection_method
+    "leaf", allow_single_cluster=True, and return_probabilities=True, which
+    returns (labels, probabilities) with scikit-learn's membership strengths
+    (a tensor of the requested precision).
     """
     min_cluster_size, min_samples, cluster_selection_epsilon = validate_parameters(
         min_cluster_size, min_samples, cluster_selection_epsilon, backend, precision)
+    cluster_selection_method, allow_single_cluster = validate_selection(cluster_selection_method,
+                                                                        allow_single_cluster)
 
     if _is_native(X):
         if not _native_is_numeric(X):
@@ -132,4 +151,13 @@ def hdbscan(
 
     from ._cuda import cluster
 
-    return cluster(X, int(min_cluster_size), int(min_samples), float(cluster_selection_epsilon), precision)
+    # The seam keeps the reference's signature (hdbscan_gpu/_api.py:92-102); the
+    # extensions travel as keywords only when they differ from its contract.
+    extras = {}
+    if cluster_selection_method != "eom":
+        extras["method"] = cluster_selection_method
+    if allow_single_cluster:
+        extras["allow_single_cluster"] = True
+    if return_probabilities:
+        extras["return_probabilities"] = True
+    return cluster(X, int(min_cluster_size), int(min_samples), float(cluster_selection_epsilon), precision, **extras)

@@ -50,7 +50,8 @@ class Plan:
     """
 
     def __init__(self, offsets, dims, *, min_cluster_size=5, min_samples=None, cluster_selection_epsilon=0.0,
-                 precision="float32", force_matrix=False, one_persistent=False, device=None):
+                 precision="float32", force_matrix=False, one_persistent=False, cluster_selection_method="eom",
+                 allow_single_cluster=False, device=None):
         if precision not in _DTYPES:
             raise ValueError("precision must be 'float32' or 'float64'")
         _require_gpu()
@@ -68,8 +69,12 @@ class Plan:
         self.epsilon = float(cluster_selection_epsilon)
         self.precision = precision
         self.torch_dtype, self.numpy_dtype, code = _DTYPES[precision]
+        if cluster_selection_method not in ("eom", "leaf"):
+            raise ValueError("cluster_selection_method must be 'eom' or 'leaf'")
         self.flags = (_lib.HDB_FLAG_FORCE_MATRIX if force_matrix else 0) | (
-            _lib.HDB_FLAG_ONE_PERSISTENT if one_persistent else 0)
+            _lib.HDB_FLAG_ONE_PERSISTENT if one_persistent else 0) | (
+            _lib.HDB_FLAG_LEAF if cluster_selection_method == "leaf" else 0) | (
+            _lib.HDB_FLAG_ALLOW_SINGLE if allow_single_cluster else 0)
         lib = _lib.lib()
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -100,11 +105,13 @@ class Plan:
     def workspace(self) -> torch.Tensor:
         return torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8, device=self.device)
 
-    def export_buffers(self, hierarchy=True, gradients=False) -> dict:
-        """Device tensors for hdb_exports_t (edges, linkage, condensed tree, cores)."""
+    def export_buffers(self, hierarchy=True, gradients=False, probabilities=False) -> dict:
+        """Device tensors for hdb_exports_t (edges, linkage, condensed tree, cores, probabilities)."""
         dev, dt = self.device, self.torch_dtype
         E, T, B = max(self.edges, 1), max(self.points, 1), self.windows
         out = {}
+        if probabilities:
+            out["probabilities"] = torch.empty(T, dtype=dt, device=dev)
         if hierarchy or gradients:
             out.update(
                 edges_uv=torch.empty((E, 2), dtype=torch.int32, device=dev),
@@ -203,16 +210,18 @@ _plan_lock = threading.Lock()
 _plans: "OrderedDict[tuple, Plan]" = OrderedDict()
 
 
-def plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, force_matrix=False) -> Plan:
+def plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, force_matrix=False, method="eom",
+             allow_single_cluster=False) -> Plan:
     """Cached Plan for these window sizes and parameters on the current device."""
     offsets = np.asarray(offsets, dtype=np.int64)
     key = (torch.cuda.current_device(), offsets.tobytes(), int(dims), int(min_cluster_size), int(min_samples),
-           float(epsilon), precision, bool(force_matrix))
+           float(epsilon), precision, bool(force_matrix), method, bool(allow_single_cluster))
     with _plan_lock:
         plan = _plans.get(key)
         if plan is None:
             plan = Plan(offsets, dims, min_cluster_size=min_cluster_size, min_samples=min_samples,
-                        cluster_selection_epsilon=epsilon, precision=precision, force_matrix=force_matrix)
+                        cluster_selection_epsilon=epsilon, precision=precision, force_matrix=force_matrix,
+                        cluster_selection_method=method, allow_single_cluster=allow_single_cluster)
             _plans[key] = plan
             if len(_plans) > 32:
                 _plans.popitem(last=False)
@@ -234,7 +243,8 @@ def to_device_tensor(X, precision) -> torch.Tensor:
     return torch.from_numpy(host).to(device="cuda")
 
 
-def cluster(x, min_cluster_size, min_samples, epsilon, precision):
+def cluster(x, min_cluster_size, min_samples, epsilon, precision, method="eom", allow_single_cluster=False,
+            return_probabilities=False):
     """Labels for [N, D] or [B, N, D] input (the reference's backend seam)."""
     _require_gpu()
     X = to_device_tensor(x, precision)
@@ -244,11 +254,17 @@ def cluster(x, min_cluster_size, min_samples, epsilon, precision):
             X = X[None]
         batch, n, dims = X.shape
         offsets = np.arange(batch + 1, dtype=np.int64) * n
-        plan = plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision)
-        labels, status = plan.forward(X.reshape(batch * n, dims))
+        plan = plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, method=method,
+                        allow_single_cluster=allow_single_cluster)
+        exports = plan.export_buffers(hierarchy=False, probabilities=True) if return_probabilities else None
+        labels, status = plan.forward(X.reshape(batch * n, dims), exports=exports)
         raise_for_status(int(status.item()))
         labels = labels.view(batch, n)
-        return labels[0] if unbatched else labels
+        labels = labels[0] if unbatched else labels
+        if not return_probabilities:
+            return labels
+        probs = exports["probabilities"].view(batch, n)
+        return labels, (probs[0] if unbatched else probs)
 
 
 def pack(windows, precision="float32"):
@@ -265,13 +281,14 @@ def pack(windows, precision="float32"):
 
 
 def cluster_ragged(packed, offsets, min_cluster_size, min_samples, epsilon, precision, exports=False,
-                   check=True, force_matrix=False):
-    """Labels [sum N] for a ragged batch; optionally the hierarchy exports too."""
+                   check=True, force_matrix=False, method="eom", allow_single_cluster=False):
+    """Labels [sum N] for a ragged batch; optionally the hierarchy exports (with probabilities) too."""
     _require_gpu()
     X = to_device_tensor(packed, precision)
     with torch.cuda.device(X.device):
-        plan = plan_for(offsets, X.shape[1], min_cluster_size, min_samples, epsilon, precision, force_matrix)
-        buffers = plan.export_buffers(hierarchy=True, gradients=True) if exports else None
+        plan = plan_for(offsets, X.shape[1], min_cluster_size, min_samples, epsilon, precision, force_matrix,
+                        method=method, allow_single_cluster=allow_single_cluster)
+        buffers = plan.export_buffers(hierarchy=True, gradients=True, probabilities=True) if exports else None
         labels, status = plan.forward(X, exports=buffers)
         if check:
             raise_for_status(int(status.item()))

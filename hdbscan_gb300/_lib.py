@@ -16,6 +16,8 @@ HDB_F64 = 1
 HDB_FLAG_FORCE_MATRIX = 1
 HDB_FLAG_NO_GRAPH_STREAMS = 2
 HDB_FLAG_ONE_PERSISTENT = 4
+HDB_FLAG_LEAF = 8
+HDB_FLAG_ALLOW_SINGLE = 16
 STATUS_OVERFLOW = 1
 STATUS_NONFINITE = 2
 STATUS_INTERNAL = 4
@@ -25,7 +27,8 @@ _lock = threading.Lock()
 _lib = None
 
 EXPORT_FIELDS = ("edges_uv", "edge_w", "order", "link_lr", "link_w", "link_size", "n_clusters", "cl_parent",
-                 "cl_birth", "cl_stability", "cl_selected", "point_parent", "core", "core_nbr", "stage_ns")
+                 "cl_birth", "cl_stability", "cl_selected", "point_parent", "core", "core_nbr", "stage_ns",
+                 "probabilities")
 
 
 class Exports(ctypes.Structure):

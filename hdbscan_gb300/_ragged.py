@@ -4,22 +4,24 @@ from __future__ import annotations
 
 import numpy as np
 
-from ._api import validate_limits, validate_parameters
+from ._api import validate_limits, validate_parameters, validate_selection
 
 
 def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=5, min_samples=None,
                    cluster_selection_epsilon=0.0, precision="float32", return_hierarchy=False,
-                   force_matrix=False):
+                   force_matrix=False, cluster_selection_method="eom", allow_single_cluster=False):
     """Cluster a ragged batch in one launch.
 
     Give either `windows` (a list of [N_i, D] arrays/tensors) or `packed`
     ([sum N_i, D]) with `offsets` ([B+1] row offsets).  Returns
     (labels [sum N_i] int32 CUDA tensor, offsets) and, with
     return_hierarchy=True, a dict of device exports (Prim edges, sort order,
-    single-linkage rows, condensed clusters, cores).
+    single-linkage rows, condensed clusters, cores, membership probabilities).
     """
     min_cluster_size, min_samples, cluster_selection_epsilon = validate_parameters(
         min_cluster_size, min_samples, cluster_selection_epsilon, "cuda", precision)
+    cluster_selection_method, allow_single_cluster = validate_selection(cluster_selection_method,
+                                                                        allow_single_cluster)
     from ._cuda import cluster_ragged, pack, to_device_tensor
 
     if windows is not None:
@@ -41,7 +43,8 @@ def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=
         raise ValueError("min_samples must not exceed the number of samples")
     result = cluster_ragged(packed, offsets, int(min_cluster_size), int(min_samples),
                             float(cluster_selection_epsilon), precision, exports=return_hierarchy,
-                            force_matrix=force_matrix)
+                            force_matrix=force_matrix, method=cluster_selection_method,
+                            allow_single_cluster=allow_single_cluster)
     if return_hierarchy:
         labels, exports = result
         return labels, offsets, exports

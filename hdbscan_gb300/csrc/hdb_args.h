@@ -46,6 +46,9 @@ struct ForwardArgs {
     uint8_t* cl_selected;      // [T]
     int32_t* point_parent;     // [T]
     int64_t* stage_ns;         // [B, 8] globaltimer at stage boundaries (diagnostics)
+    void* probabilities;       // [T] membership strengths (Real)
+    int method;                // cluster selection: 0 excess of mass, 1 leaf
+    int allow_single;          // the root may be selected
 };
 
 struct DistanceArgs {

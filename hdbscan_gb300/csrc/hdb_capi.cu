@@ -567,6 +567,9 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.cl_selected = ex->cl_selected;
         a.point_parent = ex->point_parent;
         a.stage_ns = ex->stage_ns;
+        a.probabilities = ex->probabilities;
+        a.method = (p->flags & HDB_FLAG_LEAF) ? 1 : 0;
+        a.allow_single = (p->flags & HDB_FLAG_ALLOW_SINGLE) ? 1 : 0;
         HDB_CUDA(c.fv->launch(a, c.grid, c.smem, s, c.priority));
         if (fork) HDB_CUDA(cudaEventRecord(p->events[2 * i + 1], s));
     }

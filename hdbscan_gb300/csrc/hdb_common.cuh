@@ -31,6 +31,7 @@ template <> struct RealTraits<float> {
     __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
     __device__ __forceinline__ static float sqrt_rn(float a) { return __fsqrt_rn(a); }
     __device__ __forceinline__ static float recip(float a) { return __fdiv_rn(1.0f, a); }
+    __device__ __forceinline__ static float div(float a, float b) { return __fdiv_rn(a, b); }
     __device__ __forceinline__ static float maxr(float a, float b) { return fmaxf(a, b); }
     // Order-preserving key for non-negative values; NaN and -0 are folded so
     // the key is total and below the "in tree" sentinel.
@@ -53,6 +54,7 @@ template <> struct RealTraits<double> {
     __device__ __forceinline__ static double add(double a, double b) { return __dadd_rn(a, b); }
     __device__ __forceinline__ static double sqrt_rn(double a) { return __dsqrt_rn(a); }
     __device__ __forceinline__ static double recip(double a) { return __ddiv_rn(1.0, a); }
+    __device__ __forceinline__ static double div(double a, double b) { return __ddiv_rn(a, b); }
     __device__ __forceinline__ static double maxr(double a, double b) { return fmax(a, b); }
     __device__ __forceinline__ static Bits key(double a) {
         return (Bits)__double_as_longlong(a) & 0x7fffffffffffffffull;

@@ -344,7 +344,8 @@ __device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char*
         }
     }
     __syncwarp();
-    select_and_label_warp<Real>(a, n, next_label, epsilon, args.labels + base);
+    select_and_label_warp<Real>(a, n, next_label, epsilon, args.method, args.allow_single != 0, args.labels + base,
+                                args.probabilities ? static_cast<Real*>(args.probabilities) + base : nullptr);
     if (args.cl_parent) {
         for (int c = lane; c < next_label - n; c += 32) {
             static_cast<Real*>(args.cl_stability)[base + c] = a.r2[c];

@@ -380,8 +380,11 @@ __device__ void linkage_warp(const Arena<Real>& a, int n) {
 // level per warp round.  Linkage node ids n..2n-2 (index id-n); cluster ids
 // n.. (index id-n).  Inputs: s4 left, s5 right, s6 size, r0 merge weights
 // (turned into lambda = 1/weight in place).  Outputs: s2 cluster parent, r1
-// birth, r2 stability, sel, s9 point parent.  Returns next_label
-// (warp-uniform).
+// birth, r2 stability, sel, s9 point parent, s8 the linkage node each point
+// was pruned at (its lambda is lambda[s8 - n]), s3 the deepest linkage node of
+// each cluster (index id - n; lambda there is the largest lambda leaving the
+// cluster, as lambda never decreases down a cluster's path).  Returns
+// next_label (warp-uniform).
 // ---------------------------------------------------------------------------
 template <typename Real>
 __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
@@ -434,6 +437,7 @@ __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
             const int label0 = next_label + 2 * __popc(b2 & lt);
             if (valid) {
                 const int ci = cluster - n;
+                a.s3[ci] = (int16_t)(queue[q] - n);  // deeper levels overwrite: the cluster's last node
                 const Real cb = birth[ci];
                 Real st = stab[ci];
                 if (split) {
@@ -480,50 +484,68 @@ __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
         int v = dparent[i];
         while (v != root && size[v - n] < mcs) v = dparent[v];
         a.s9[i] = relabel[v - n];
+        a.s8[i] = (int16_t)v;
     }
     __syncwarp();
     return next_label;
 }
 
 // ---------------------------------------------------------------------------
-// Excess of mass (reference: _kernels.py:672-710, binary form :648-669) and
-// epsilon merge + labels (reference: _kernels.py:712-760).  Writes
-// labels[0..n) through `labels` (global memory).
+// Cluster selection and labels.  method 0: excess of mass (reference:
+// _kernels.py:672-710, binary form :648-669), 1: leaf clusters; allow_single
+// lets the root compete; epsilon merge and labels (reference:
+// _kernels.py:712-760).  The leaf and allow_single options and the
+// probabilities restate scikit-learn's selection (sklearn/cluster/_hdbscan/
+// _tree.pyx:433-554, 644-799); with method 0 and allow_single false this is
+// exactly the reference's path.  Writes labels[0..n) and, when non-null,
+// probabilities[0..n) (global memory).
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_label, Real epsilon,
-                                      int32_t* labels) {
+__device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_label, Real epsilon, int method,
+                                      bool allow_single, int32_t* labels, Real* probabilities) {
+    using T = RealTraits<Real>;
     const int lane = threadIdx.x & 31;
     const int clusters = next_label - n;
+    const bool splits = clusters > 1;
+    const bool eps_on = epsilon > Real(0) && splits;
     const int16_t* parent = a.s2;
     const Real* birth = a.r1;
+    const Real* lam = a.r0;
     Real* stab = a.r2;
-    int16_t* first = a.s3;
+    int16_t* first = a.s0;             // first child cluster (children come in consecutive pairs)
+    int16_t* resolved = a.s1;          // nearest selected cluster at or above each cluster, -1 none
+    const int16_t* last_node = a.s3;   // deepest linkage node of each cluster
+    int16_t* blocked = a.s4;
+    int16_t* stop = a.s5;
+    int16_t* label_map = a.s6;
     for (int c = lane; c < clusters; c += 32) first[c] = -1;
     __syncwarp();
-    // Children come in consecutive pairs (n+1, n+2), (n+3, n+4), ...
     for (int child = n + 1 + 2 * lane; child < next_label; child += 64) first[parent[child - n] - n] = (int16_t)child;
     __syncwarp();
+    int single_root = 0;
     if (lane == 0) {
-        // 1. Excess of mass, children (larger ids) before parents.
-        for (int node = next_label - 1; node > n; --node) {
-            const int f = first[node - n];
-            const Real subtree = f < 0 ? Real(0)
-                                       : RealTraits<Real>::add(RealTraits<Real>::add(Real(0), stab[f - n]),
-                                                               stab[f + 1 - n]);
-            if (subtree > stab[node - n]) {
-                a.sel[node - n] = 0;
-                stab[node - n] = subtree;
+        // 1. Candidates: excess of mass, children (larger ids) before parents;
+        //    or the leaves of the cluster tree (none if the root never splits).
+        if (method == 0) {
+            a.sel[0] = allow_single ? 1 : 0;
+            for (int node = next_label - 1; node >= (allow_single ? n : n + 1); --node) {
+                const int f = first[node - n];
+                const Real subtree = f < 0 ? Real(0) : T::add(T::add(Real(0), stab[f - n]), stab[f + 1 - n]);
+                if (subtree > stab[node - n]) {
+                    a.sel[node - n] = 0;
+                    stab[node - n] = subtree;
+                }
             }
+        } else {
+            a.sel[0] = 0;
+            for (int node = n + 1; node < next_label; ++node) a.sel[node - n] = first[node - n] < 0 ? 1 : 0;
         }
         // 2. Parents first (ascending ids): suppress the descendants of a
         //    selected cluster; with epsilon, mark the cluster each surviving
-        //    selection resolves to (itself, or its epsilon stop ancestor).
-        int16_t* blocked = a.s4;
-        int16_t* stop = a.s5;
-        int16_t* label_map = a.s6;
-        blocked[0] = 0;
-        label_map[0] = -1;
+        //    selection resolves to (itself, or its epsilon stop ancestor; the
+        //    climb ends below the root, at the root with allow_single).
+        blocked[0] = a.sel[0];
+        label_map[0] = (eps_on && a.sel[0]) ? 1 : -1;  // 1/birth(root) = inf: the root never climbs
         for (int node = n + 1; node < next_label; ++node) {
             const int anc = parent[node - n];
             const int inherited = blocked[anc - n];
@@ -532,30 +554,52 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
             if (inherited) selected = 0;
             a.sel[node - n] = (uint8_t)selected;
             label_map[node - n] = -1;
-            if (epsilon > Real(0)) {
-                const int st = anc == n ? node
-                                        : (RealTraits<Real>::recip(birth[anc - n]) > epsilon ? anc : stop[anc - n]);
+            if (eps_on) {
+                const int st = anc == n ? (allow_single ? n : node)
+                                        : (T::recip(birth[anc - n]) > epsilon ? anc : stop[anc - n]);
                 stop[node - n] = (int16_t)st;
                 if (selected) {
-                    const int chosen = RealTraits<Real>::recip(birth[node - n]) < epsilon ? st : node;
+                    const int chosen = T::recip(birth[node - n]) < epsilon ? st : node;
                     label_map[chosen - n] = 1;
                 }
             }
         }
-        // 3. Ascending: final selection, label numbers, label of every cluster.
-        int16_t* resolved = a.s7;
-        resolved[0] = -1;
+        // 3. Ascending: final selection, label numbers (the root first when
+        //    selected), nearest selected cluster of every cluster.
         int label = 0;
-        for (int node = n + 1; node < next_label; ++node) {
-            const int selected = epsilon > Real(0) ? (label_map[node - n] == 1) : a.sel[node - n];
+        for (int node = n; node < next_label; ++node) {
+            const int selected = eps_on ? (label_map[node - n] == 1) : a.sel[node - n];
             a.sel[node - n] = (uint8_t)selected;
-            const int lm = selected ? label++ : -1;
-            label_map[node - n] = (int16_t)lm;
-            resolved[node - n] = (int16_t)(selected ? lm : resolved[parent[node - n] - n]);
+            label_map[node - n] = (int16_t)(selected ? label++ : -1);
+            resolved[node - n] = (int16_t)(selected ? node : (node == n ? -1 : resolved[parent[node - n] - n]));
+        }
+        single_root = allow_single && label == 1 && a.sel[0];
+    }
+    single_root = __shfl_sync(0xffffffffu, single_root, 0);
+    __syncwarp();
+    // Points: the nearest selected cluster's label; below a lone selected root
+    // (allow_single) a point joins at lambda >= 1/eps, or >= the largest
+    // lambda leaving the root when eps = 0 (_tree.pyx:491-508); else noise.
+    const Real threshold = epsilon != Real(0) ? T::recip(epsilon) : lam[last_node[0]];
+    for (int i = lane; i < n; i += 32) {
+        const int c = resolved[a.s9[i] - n];
+        const Real lambda_i = lam[a.s8[i] - n];
+        int lab = -1;
+        if (c > n) lab = label_map[c - n];
+        else if (c == n && single_root && lambda_i >= threshold) lab = label_map[0];
+        labels[i] = lab;
+        if (probabilities) {
+            // Membership strength (_tree.pyx:515-554): the point's lambda over
+            // the largest lambda leaving its cluster, capped at 1.
+            Real prob = Real(0);
+            if (lab >= 0) {
+                const Real max_lambda = lam[last_node[c - n]];
+                if (max_lambda == Real(0) || isinf(lambda_i)) prob = Real(1);
+                else prob = T::div(lambda_i < max_lambda ? lambda_i : max_lambda, max_lambda);
+            }
+            probabilities[i] = prob;
         }
     }
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) labels[i] = a.s7[a.s9[i] - n];
     __syncwarp();
 }
 

@@ -58,6 +58,11 @@ extern "C" {
 #define HDB_FLAG_NO_GRAPH_STREAMS 2u /* run all window classes on the caller's stream */
 #define HDB_FLAG_ONE_PERSISTENT 4u /* one persistent CTA (or cluster) per window class: every window of a
                                       class passes through the same CTAs (queue and hand-off tests) */
+/* Cluster selection beyond the reference's fixed contract (excess of mass, no
+ * single cluster), as scikit-learn's HDBSCAN(cluster_selection_method=,
+ * allow_single_cluster=) defines them (sklearn/cluster/_hdbscan/_tree.pyx). */
+#define HDB_FLAG_LEAF 8u           /* cluster_selection_method="leaf" */
+#define HDB_FLAG_ALLOW_SINGLE 16u  /* allow_single_cluster=True */
 
 typedef struct hdb_plan hdb_plan_t;
 
@@ -82,6 +87,7 @@ typedef struct hdb_exports {
     int32_t* core_nbr;     /* [T]   ms-th nearest neighbour in (distance, index) order */
     int64_t* stage_ns;     /* [B,8] device timestamps (ns) per window: start, Prim start, Prim end,
                                     hierarchy start, sort end, linkage end, condensation end, labels end */
+    void* probabilities;   /* [T]   membership strength in [0, 1] (Real), scikit-learn's probabilities_ */
 } hdb_exports_t;
 
 /* Library version (HDB_VERSION). */

@@ -161,7 +161,8 @@ void FN(hdb_oracle_argsort)(const REAL* w, int m, int32_t* order, int depth_over
  *   cl_parent/cl_birth/cl_stability/cl_selected/cl_size[n]   indexed by id - n
  *   point_parent[n], point_lambda[n]  condensed id each point falls out of, and at which lambda
  *   core[n]                         self-inclusive core distances (k = ms-1)
- *   core_nbr[n]                     lowest index j != i with d(i,j) == core (or -1) */
+ *   core_nbr[n]                     lowest index j != i with d(i,j) == core (or -1)
+ *   probabilities[n]                membership strength of each point (0 for noise) */
 typedef struct {
     int32_t* labels;
     int32_t* edges_uv;
@@ -180,13 +181,19 @@ typedef struct {
     REAL* point_lambda;
     REAL* core;
     int32_t* core_nbr;
+    REAL* probabilities;
 } FN(hdb_oracle_out);
 
 /* Graph stage: dense distance matrix + core distances -> hierarchy and labels.
  * core == NULL means the unit-core case (ms <= 2) where the mutual
- * reachability weight is the distance itself. */
-void FN(hdb_oracle_graph)(const REAL* dist, const REAL* core, int n, int mcs, double eps_in,
-                          const FN(hdb_oracle_out)* out) {
+ * reachability weight is the distance itself.
+ * method 0 = excess of mass (the reference's only method), 1 = leaf;
+ * allow_single != 0 lets the root be selected.  Both extensions restate
+ * scikit-learn's cluster selection (sklearn/cluster/_hdbscan/_tree.pyx:644-799,
+ * _do_labelling :433-512); with method 0 and allow_single 0 this is exactly
+ * the reference's path. */
+void FN(hdb_oracle_graph_ex)(const REAL* dist, const REAL* core, int n, int mcs, double eps_in, int method,
+                             int allow_single, const FN(hdb_oracle_out)* out) {
     const REAL epsilon = (REAL)eps_in; /* options array is cast to the precision, _cuda.py:105 */
     const int unit_core = core == NULL;
     int m = n - 1;
@@ -341,58 +348,109 @@ void FN(hdb_oracle_graph)(const REAL* dist, const REAL* core, int n, int mcs, do
         }
     }
 
-    /* Excess-of-mass selection.  _kernels.py:672-710: children are summed in
-     * ascending id order, a node whose children's sum is strictly larger is
-     * deselected and inherits the sum; then every descendant of a selected
-     * node is suppressed in one forward pass (parents have smaller ids). */
+    /* Cluster selection.
+     * Excess of mass, _kernels.py:672-710: children are summed in ascending id
+     * order, a node whose children's sum is strictly larger is deselected and
+     * inherits the sum; then every descendant of a selected node is suppressed
+     * in one forward pass (parents have smaller ids).  With allow_single the
+     * root takes part like any other cluster (_tree.pyx:704-708, 727-739).
+     * Leaf, _tree.pyx:761-781: the clusters without child clusters; none when
+     * the root never splits. */
+    const int root = n;
+    const int splits = next_label > root + 1;
     {
-        for (int node = next_label - 1; node > n; --node) {
-            REAL subtree = 0;
-            for (int child = node + 1; child < next_label; ++child)
-                if (parent[child] == node) subtree += stability[child];
-            if (subtree > stability[node]) {
-                selected[node] = 0;
-                stability[node] = subtree;
+        if (method == 0) {
+            if (allow_single) selected[root] = 1;
+            for (int node = next_label - 1; node >= (allow_single ? root : root + 1); --node) {
+                REAL subtree = 0;
+                for (int child = node + 1; child < next_label; ++child)
+                    if (parent[child] == node) subtree += stability[child];
+                if (subtree > stability[node]) {
+                    selected[node] = 0;
+                    stability[node] = subtree;
+                }
             }
+            uint8_t* blocked = (uint8_t*)calloc((size_t)nodes, 1);
+            blocked[root] = selected[root];
+            for (int node = n + 1; node < next_label; ++node) {
+                int inherited = blocked[parent[node]];
+                blocked[node] = (uint8_t)(inherited || selected[node]);
+                if (inherited) selected[node] = 0;
+            }
+            free(blocked);
+        } else {
+            uint8_t* has_child = (uint8_t*)calloc((size_t)nodes, 1);
+            for (int node = n + 1; node < next_label; ++node) has_child[parent[node]] = 1;
+            selected[root] = 0;
+            for (int node = n + 1; node < next_label; ++node) selected[node] = !has_child[node];
+            free(has_child);
         }
-        uint8_t* blocked = (uint8_t*)calloc((size_t)nodes, 1);
-        for (int node = n + 1; node < next_label; ++node) {
-            int inherited = blocked[parent[node]];
-            blocked[node] = (uint8_t)(inherited || selected[node]);
-            if (inherited) selected[node] = 0;
-        }
-        free(blocked);
     }
 
-    /* Epsilon merge and labelling.  _kernels.py:712-760: a selected cluster
-     * with 1/birth < eps climbs to its first ancestor with 1/birth > eps (the
-     * root's children stop the climb); labels number the surviving clusters by
-     * ascending id; every point takes the label of its nearest selected
-     * ancestor, -1 if none. */
+    /* Epsilon merge, _kernels.py:712-760: a selected cluster with 1/birth <
+     * eps climbs to its first ancestor with 1/birth > eps; the climb stops
+     * below the root (at the root with allow_single, _tree.pyx:578-603).
+     * Skipped when the root never splits (_tree.pyx:741).  Every selected
+     * cluster marks the cluster it resolves to (the reference's rule). */
+    int32_t* resolved_cluster = (int32_t*)malloc(sizeof(int32_t) * (size_t)nodes);
     {
-        if (epsilon > 0) {
+        if (epsilon > 0 && splits) {
             int32_t* stop = (int32_t*)malloc(sizeof(int32_t) * (size_t)nodes);
+            uint8_t* chosen_mark = (uint8_t*)calloc((size_t)nodes, 1);
+            stop[root] = root;
+            if (selected[root]) chosen_mark[root] = 1;  /* 1/birth(root) = inf: never climbs */
             for (int node = n + 1; node < next_label; ++node) {
                 int ancestor = parent[node];
-                stop[node] = ancestor == n ? node
+                stop[node] = ancestor == root ? (allow_single ? root : node)
                            : ((REAL)1 / birth[ancestor] > epsilon ? ancestor : stop[ancestor]);
                 if (!selected[node]) continue;
                 int chosen = (REAL)1 / birth[node] < epsilon ? stop[node] : node;
-                label_map[chosen] = 1;
+                chosen_mark[chosen] = 1;
             }
-            for (int node = n + 1; node < next_label; ++node) selected[node] = label_map[node] == 1;
+            for (int node = root; node < next_label; ++node) selected[node] = chosen_mark[node];
             free(stop);
+            free(chosen_mark);
         }
-        int label = 0;
+        /* Labels number the selected clusters by ascending id (the root first
+         * when selected, _tree.pyx:785); every point takes its nearest selected
+         * ancestor; a point whose nearest one is the root is noise unless the
+         * root is the only cluster (allow_single), when it joins at lambda >=
+         * 1/eps, or >= the largest lambda leaving the root when eps = 0
+         * (_tree.pyx:491-508). */
+        int label = 0, count = 0;
+        for (int node = root; node < next_label; ++node) {
+            label_map[node] = selected[node] ? label++ : -1;
+            count += selected[node];
+        }
+        resolved_cluster[root] = selected[root] ? root : -1;
         for (int node = n + 1; node < next_label; ++node)
-            if (selected[node]) label_map[node] = label++;
-        int32_t* resolved = relabel; /* linkage relabelling is dead here */
-        resolved[n] = -1;
+            resolved_cluster[node] = selected[node] ? node : resolved_cluster[parent[node]];
+        REAL* deaths = (REAL*)calloc((size_t)nodes, sizeof(REAL));  /* largest lambda leaving each cluster */
+        for (int i = 0; i < n; ++i) deaths[pparent[i]] = deaths[pparent[i]] > plambda[i] ? deaths[pparent[i]] : plambda[i];
         for (int node = n + 1; node < next_label; ++node)
-            resolved[node] = selected[node] ? label_map[node] : resolved[parent[node]];
-        if (out->labels)
-            for (int i = 0; i < n; ++i) out->labels[i] = resolved[pparent[i]];
+            deaths[parent[node]] = deaths[parent[node]] > birth[node] ? deaths[parent[node]] : birth[node];
+        const int single_root = allow_single && count == 1 && selected[root];
+        const REAL threshold = epsilon != 0 ? (REAL)1 / epsilon : deaths[root];
+        for (int i = 0; i < n; ++i) {
+            int c = resolved_cluster[pparent[i]];
+            int lab = -1;
+            if (c > root) lab = label_map[c];
+            else if (c == root && single_root && plambda[i] >= threshold) lab = label_map[root];
+            if (out->labels) out->labels[i] = lab;
+            /* Membership strength, _tree.pyx:515-554. */
+            if (out->probabilities) {
+                REAL prob = 0;
+                if (lab >= 0) {
+                    const REAL max_lambda = deaths[c];
+                    if (max_lambda == 0 || isinf((double)plambda[i])) prob = 1;
+                    else prob = (plambda[i] < max_lambda ? plambda[i] : max_lambda) / max_lambda;
+                }
+                out->probabilities[i] = prob;
+            }
+        }
+        free(deaths);
     }
+    free(resolved_cluster);
 
     if (out->edges_uv) for (int i = 0; i < m; ++i) { out->edges_uv[2 * i] = eu[i]; out->edges_uv[2 * i + 1] = ev[i]; }
     if (out->edge_w) for (int i = 0; i < m; ++i) out->edge_w[i] = ew[i];
@@ -417,11 +475,16 @@ void FN(hdb_oracle_graph)(const REAL* dist, const REAL* core, int n, int mcs, do
     free(selected); free(pparent); free(plambda); free(label_map);
 }
 
+void FN(hdb_oracle_graph)(const REAL* dist, const REAL* core, int n, int mcs, double eps_in,
+                          const FN(hdb_oracle_out)* out) {
+    FN(hdb_oracle_graph_ex)(dist, core, n, mcs, eps_in, 0, 0, out);
+}
+
 /* Full per-window pipeline from points.  Returns the window status (0 ok,
  * 1 distance overflow, 2 non-finite input; 2 outranks 1 as the host checks at
  * _cuda.py:98-99 run before those at :112-113).  out may be NULL. */
-int FN(hdb_oracle_cluster)(const REAL* x, int n, int d, int mcs, int ms, double eps,
-                           const FN(hdb_oracle_out)* out) {
+int FN(hdb_oracle_cluster_ex)(const REAL* x, int n, int d, int mcs, int ms, double eps, int method,
+                              int allow_single, const FN(hdb_oracle_out)* out) {
     FN(hdb_oracle_out) none;
     memset(&none, 0, sizeof(none));
     if (!out) out = &none;
@@ -446,10 +509,15 @@ int FN(hdb_oracle_cluster)(const REAL* x, int n, int d, int mcs, int ms, double 
                     if (j != i && dist[(size_t)i * n + j] == core[i]) { out->core_nbr[i] = j; break; }
             }
         }
-        FN(hdb_oracle_graph)(dist, unit_core ? NULL : core, n, mcs, eps, out);
+        FN(hdb_oracle_graph_ex)(dist, unit_core ? NULL : core, n, mcs, eps, method, allow_single, out);
     }
     free(dist); free(core); free(rowbuf);
     return status;
+}
+
+int FN(hdb_oracle_cluster)(const REAL* x, int n, int d, int mcs, int ms, double eps,
+                           const FN(hdb_oracle_out)* out) {
+    return FN(hdb_oracle_cluster_ex)(x, n, d, mcs, ms, eps, 0, 0, out);
 }
 
 typedef struct {

@@ -50,6 +50,10 @@ def lib():
                 fn.restype = ctypes.c_int
                 fn.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                ctypes.POINTER(_Out)]
+                fn = getattr(handle, f"hdb_oracle_cluster_ex_{suffix}")
+                fn.restype = ctypes.c_int
+                fn.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Out)]
                 fn = getattr(handle, f"hdb_oracle_graph_{suffix}")
                 fn.restype = None
                 fn.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_Out)]
@@ -99,7 +103,8 @@ def argsort(weights, precision=None, depth=None):
 
 _FIELDS = ("labels", "edges_uv", "edge_w", "order", "link_lr", "link_w", "link_size", "n_clusters",
            "cl_parent", "cl_birth", "cl_stability", "cl_selected", "cl_size", "point_parent", "point_lambda",
-           "core", "core_nbr")
+           "core", "core_nbr", "probabilities")
+METHODS = {"eom": 0, "leaf": 1}
 
 
 class _Out(ctypes.Structure):
@@ -126,6 +131,7 @@ def _outputs(n, dtype):
         "point_lambda": np.empty(n, dtype),
         "core": np.empty(n, dtype),
         "core_nbr": np.empty(n, np.int32),
+        "probabilities": np.empty(n, dtype),
     }
     struct = _Out(*[out[name].ctypes.data for name in _FIELDS])
     return out, struct
@@ -140,8 +146,12 @@ def _trim(out, n):
     return out
 
 
-def cluster(x, min_cluster_size, min_samples=None, epsilon=0.0, precision="float64"):
-    """Run the whole reference pipeline on one window and return every stage's state."""
+def cluster(x, min_cluster_size, min_samples=None, epsilon=0.0, precision="float64", method="eom",
+            allow_single_cluster=False):
+    """Run the whole reference pipeline on one window and return every stage's state.
+
+    method "leaf" and allow_single_cluster=True are the scikit-learn selection
+    options beyond the reference's fixed contract (eom, no single cluster)."""
     dtype, suffix = _dtype(precision)
     x = np.ascontiguousarray(x, dtype=dtype)
     if x.ndim != 2:
@@ -149,8 +159,9 @@ def cluster(x, min_cluster_size, min_samples=None, epsilon=0.0, precision="float
     n, d = x.shape
     ms = min_cluster_size if min_samples is None else min_samples
     out, struct = _outputs(n, dtype)
-    status = getattr(lib(), f"hdb_oracle_cluster_{suffix}")(
-        _ptr(x), n, d, int(min_cluster_size), int(ms), float(epsilon), ctypes.byref(struct))
+    status = getattr(lib(), f"hdb_oracle_cluster_ex_{suffix}")(
+        _ptr(x), n, d, int(min_cluster_size), int(ms), float(epsilon), METHODS[method],
+        int(bool(allow_single_cluster)), ctypes.byref(struct))
     out["status"] = int(status)
     return _trim(out, n)
 

@@ -8,7 +8,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-FAMILIES = ("known", "corpus", "exhaustive", "sweep", "sort", "configs")
+FAMILIES = ("known", "corpus", "exhaustive", "sweep", "sort", "configs", "selection")
 
 
 @lru_cache(maxsize=None)

@@ -93,18 +93,22 @@ class Reference:
         return out
 
 
-def sklearn_fit(x, mcs, ms, eps):
+def sklearn_fit(x, mcs, ms, eps, method="eom", allow_single=False):
     from sklearn.cluster import HDBSCAN
     from sklearn.cluster._hdbscan._tree import _condense_tree
 
-    h = HDBSCAN(algorithm="auto", metric="euclidean", cluster_selection_method="eom", allow_single_cluster=False,
-                alpha=1.0, copy=True, min_cluster_size=mcs, min_samples=ms, cluster_selection_epsilon=eps)
+    h = HDBSCAN(algorithm="auto", metric="euclidean", cluster_selection_method=method,
+                allow_single_cluster=allow_single, alpha=1.0, copy=True, min_cluster_size=mcs, min_samples=ms,
+                cluster_selection_epsilon=eps)
     out = {}
     try:
         out["labels"] = h.fit_predict(np.asarray(x, dtype=np.float64)).astype(np.int32)
-    except TypeError:
+        out["probabilities"] = np.asarray(h.probabilities_, np.float64)
+    except (TypeError, KeyError):
         # scikit-learn 1.9.0 with NumPy >= 2.5 raises in epsilon_search's
-        # traverse_upwards; the linkage below is computed before that point.
+        # traverse_upwards, and _do_labelling raises KeyError when
+        # allow_single_cluster meets one selected non-root cluster and a point
+        # that reaches the root; the linkage below is computed before that.
         out["failed"] = np.int8(1)
     slt = getattr(h, "_single_linkage_tree_", None)
     if slt is not None:
@@ -122,6 +126,29 @@ def sklearn_fit(x, mcs, ms, eps):
 # ---------------------------------------------------------------------------
 # Case families.  Every input is drawn from a seed recorded here.
 # ---------------------------------------------------------------------------
+def corpus_inputs():
+    return [(name, x) for name, x in _corpus_cases().items()]
+
+
+def _corpus_cases():
+    rng = np.random.default_rng(20261203)
+    sep = np.concatenate([rng.normal(c, 0.08, (24, 2)) for c in ((-3, -3), (0, 3), (3, -3))])
+    return {
+        "separated": sep,
+        "overlap": np.concatenate([rng.normal(c, 0.45, (30, 2)) for c in ((-0.5, 0), (0.5, 0), (0, 0.8))]),
+        "density": np.concatenate([rng.normal(c, s, (k, 2)) for c, s, k in
+                                   (((-4, 0), 0.025, 30), ((0, 4), 0.3, 35), ((4, 0), 0.8, 40))]),
+        "quantized3d": rng.integers(-12, 13, (48, 3)) / 8.0,
+        "duplicates": np.repeat(np.array([[0, 0], [0.125, 0], [4, 0], [4.125, 0], [20, 20]]), [7, 5, 6, 8, 1], 0),
+        "identical": np.ones((24, 3)),
+        "grid5x5": np.array([(a, b) for a in range(5) for b in range(5)], float),
+        "cross": np.tile(np.array([[0, 0], [1, 0], [-1, 0], [0, 1], [0, -1]], float), (4, 1)),
+        "tiny": np.concatenate([rng.normal(c, 0.01, (k, 2)) for c, k in (((0, 0), 2), ((2, 2), 3), ((5, 0), 9))]),
+        "outliers": np.concatenate([sep, np.array([[20, 20], [-20, 20], [0, -30]])]),
+        "two": np.array([[0.0, 0.0], [1.0, 1.0]]),
+    }
+
+
 def corpus():
     rng = np.random.default_rng(20261203)
     sep = np.concatenate([rng.normal(c, 0.08, (24, 2)) for c in ((-3, -3), (0, 3), (3, -3))])
@@ -213,8 +240,28 @@ def config_windows():
                    p["cluster_selection_epsilon"])
 
 
+def selection():
+    """scikit-learn's selection options beyond the reference contract (leaf
+    selection, allow_single_cluster) and membership probabilities, with the
+    reference's own (eom, no single cluster) setting for the probabilities."""
+    base = dict(corpus_inputs())
+    rng = np.random.default_rng(20261204)
+    for seed in range(6):
+        k = 1 + seed % 4
+        centres = rng.normal(0, 3, (k, 3))
+        base[f"blobs{seed}"] = centres[rng.integers(0, k, 60)] + rng.normal(0, 0.4 + 0.1 * seed, (60, 3))
+    for name, x in base.items():
+        for mcs, ms in ((2, 2), (5, 5), (4, 2)):
+            ms = min(ms, len(x))
+            for method in ("eom", "leaf"):
+                for allow in (False, True):
+                    for eps in (0.0, 0.1):
+                        yield (f"{name}_{method}_single{int(allow)}_mcs{mcs}_ms{ms}_eps{eps}", x, mcs, ms, eps,
+                               method, allow)
+
+
 FAMILIES = {"corpus": corpus, "exhaustive": exhaustive, "sweep": sweep, "known": known_answers,
-            "sort": sort_fixtures, "configs": config_windows}
+            "sort": sort_fixtures, "configs": config_windows, "selection": selection}
 
 
 def pack(store: dict) -> dict:
@@ -249,6 +296,21 @@ def main(selected):
             continue
         store = {}
         names = []
+        if family == "selection":
+            for name, x, mcs, ms, eps, method, allow in gen():
+                names.append(name)
+                x = np.asarray(x, np.float64)
+                store[f"{name}/x"] = x
+                store[f"{name}/params"] = np.array([mcs, ms, eps], np.float64)
+                store[f"{name}/options"] = np.array([1 if method == "leaf" else 0, int(allow)], np.int32)
+                for key, value in sklearn_fit(x, mcs, ms, eps, method, allow).items():
+                    store[f"{name}/sk_{key}"] = value
+            store["_cases"] = names
+            packed = pack(store)
+            packed["_versions"] = np.array([sklearn.__version__, np.__version__, SCALAR])
+            np.savez_compressed(HERE / f"golden_{family}.npz", **packed)
+            print(family, len(names), "cases")
+            continue
         for name, x, mcs, ms, eps in gen():
             names.append(name)
             x = np.asarray(x, np.float64)

@@ -111,3 +111,27 @@ def test_default_min_samples_is_min_cluster_size(monkeypatch):
     monkeypatch.setitem(sys.modules, "hdbscan_gb300._cuda", fake)
     hdbscan(VALUES, min_cluster_size=4, backend="cuda", precision="float64", cluster_selection_epsilon=np.float64(0))
     assert calls["args"] == (4, 4, 0.0, "float64")
+
+
+@pytest.mark.parametrize("kwargs,match", [
+    (dict(cluster_selection_method="dbscan"), "cluster_selection_method"),
+    (dict(allow_single_cluster=1), "allow_single_cluster"),
+])
+def test_selection_option_validation(kwargs, match):
+    from hdbscan_gb300 import _api as api
+
+    with pytest.raises(ValueError, match=match):
+        api.hdbscan(np.zeros((4, 2)), min_cluster_size=2, **kwargs)
+
+
+def test_selection_options_reach_the_backend_only_when_set(monkeypatch):
+    from hdbscan_gb300 import _api as api
+    from hdbscan_gb300 import _cuda
+
+    seen = []
+    monkeypatch.setattr(_cuda, "cluster", lambda *args, **kwargs: seen.append(kwargs) or "ok")
+    x = np.arange(12, dtype=float).reshape(6, 2)
+    api.hdbscan(x, min_cluster_size=2)
+    api.hdbscan(x, min_cluster_size=2, cluster_selection_method="leaf", allow_single_cluster=True,
+                return_probabilities=True)
+    assert seen == [{}, {"method": "leaf", "allow_single_cluster": True, "return_probabilities": True}]

@@ -156,3 +156,30 @@ def test_golden_vectors_record_their_generators():
     for family in golden.FAMILIES:
         sk, npv, env = golden.versions(family)
         assert env.startswith("X86_V3")
+
+
+# ---------------------------------------------------------------------------
+# scikit-learn's selection options beyond the reference contract (leaf,
+# allow_single_cluster) and membership probabilities (float64, bit for bit).
+# ---------------------------------------------------------------------------
+METHOD_NAMES = {0: "eom", 1: "leaf"}
+
+
+@pytest.mark.parametrize("family,name", _cases("selection"))
+def test_oracle_selection_options_match_sklearn(family, name):
+    case = golden.load(family)[name]
+    if "sk_failed" in case:
+        pytest.skip("scikit-learn raised on this case")
+    mcs, ms, eps = case["params"]
+    method, allow = (int(v) for v in case["options"])
+    out = oracle.cluster(case["x"], int(mcs), int(ms), float(eps), "float64", method=METHOD_NAMES[method],
+                         allow_single_cluster=bool(allow))
+    np.testing.assert_array_equal(out["labels"], case["sk_labels"])
+    np.testing.assert_array_equal(out["probabilities"].view(np.uint64), case["sk_probabilities"].view(np.uint64))
+
+
+def test_default_selection_is_the_reference_contract():
+    case = golden.load("corpus")["overlap_mcs5_ms5_eps0.1"]
+    base = _run(case, "float64")
+    ext = oracle.cluster(case["x"], 5, 5, 0.1, "float64", method="eom", allow_single_cluster=False)
+    np.testing.assert_array_equal(base["labels"], ext["labels"])
