@@ -105,6 +105,7 @@ def hdbscan(
     cluster_selection_method="eom",
     allow_single_cluster=False,
     return_probabilities=False,
+    normalize=False,
 ):
     """Return device labels for Euclidean EOM HDBSCAN, excluding the root.
 
@@ -120,7 +121,10 @@ def hdbscan(
     Beyond the reference's fixed contract (its defaults): cluster_selection_method
     "leaf", allow_single_cluster=True, and return_probabilities=True, which
     returns (labels, probabilities) with scikit-learn's membership strengths
-    (a tensor of the requested precision).
+    (a tensor of the requested precision).  normalize=True L2-normalises every
+    point first (exact order: sum of squares in coordinate order, correctly
+    rounded sqrt and division; zero vectors unchanged), and torch bfloat16 /
+    float16 tensors are converted on the device by the same producer stage.
     """
     min_cluster_size, min_samples, cluster_selection_epsilon = validate_parameters(
         min_cluster_size, min_samples, cluster_selection_epsilon, backend, precision)
@@ -160,4 +164,8 @@ def hdbscan(
         extras["allow_single_cluster"] = True
     if return_probabilities:
         extras["return_probabilities"] = True
+    if not isinstance(normalize, (bool, np.bool_)):
+        raise ValueError("normalize must be a bool")
+    if normalize:
+        extras["normalize"] = True
     return cluster(X, int(min_cluster_size), int(min_samples), float(cluster_selection_epsilon), precision, **extras)

@@ -20,6 +20,8 @@ import torch
 from . import _lib
 
 _DTYPES = {"float32": (torch.float32, np.float32, _lib.HDB_F32), "float64": (torch.float64, np.float64, _lib.HDB_F64)}
+# Encoder outputs the producer stage converts on the device (exactly).
+_HALF_INPUTS = {torch.bfloat16: _lib.HDB_FLAG_INPUT_BF16, torch.float16: _lib.HDB_FLAG_INPUT_F16}
 
 
 def _stream_handle(device) -> int:
@@ -51,7 +53,7 @@ class Plan:
 
     def __init__(self, offsets, dims, *, min_cluster_size=5, min_samples=None, cluster_selection_epsilon=0.0,
                  precision="float32", force_matrix=False, one_persistent=False, cluster_selection_method="eom",
-                 allow_single_cluster=False, device=None):
+                 allow_single_cluster=False, input_dtype=None, normalize=False, device=None):
         if precision not in _DTYPES:
             raise ValueError("precision must be 'float32' or 'float64'")
         _require_gpu()
@@ -74,7 +76,11 @@ class Plan:
         self.flags = (_lib.HDB_FLAG_FORCE_MATRIX if force_matrix else 0) | (
             _lib.HDB_FLAG_ONE_PERSISTENT if one_persistent else 0) | (
             _lib.HDB_FLAG_LEAF if cluster_selection_method == "leaf" else 0) | (
-            _lib.HDB_FLAG_ALLOW_SINGLE if allow_single_cluster else 0)
+            _lib.HDB_FLAG_ALLOW_SINGLE if allow_single_cluster else 0) | (
+            _HALF_INPUTS.get(input_dtype, 0)) | (_lib.HDB_FLAG_L2_NORMALIZE if normalize else 0)
+        if input_dtype is not None and input_dtype not in _HALF_INPUTS and input_dtype != self.torch_dtype:
+            raise ValueError("input_dtype must be torch.bfloat16, torch.float16 or the compute precision")
+        self.input_dtype = self.torch_dtype if input_dtype is None else input_dtype
         lib = _lib.lib()
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -146,8 +152,8 @@ class Plan:
             raise ValueError(f"X must be a torch tensor on {self.device}")
         if tuple(X.shape) != (self.points, self.dims):
             raise ValueError(f"X must have shape [{self.points}, {self.dims}]")
-        if X.dtype != self.torch_dtype or not X.is_contiguous():
-            X = X.to(self.torch_dtype).contiguous()
+        if X.dtype != self.input_dtype or not X.is_contiguous():
+            X = X.to(self.input_dtype).contiguous()
         return X
 
     # -- forward ---------------------------------------------------------------
@@ -211,17 +217,19 @@ _plans: "OrderedDict[tuple, Plan]" = OrderedDict()
 
 
 def plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, force_matrix=False, method="eom",
-             allow_single_cluster=False) -> Plan:
+             allow_single_cluster=False, input_dtype=None, normalize=False) -> Plan:
     """Cached Plan for these window sizes and parameters on the current device."""
     offsets = np.asarray(offsets, dtype=np.int64)
     key = (torch.cuda.current_device(), offsets.tobytes(), int(dims), int(min_cluster_size), int(min_samples),
-           float(epsilon), precision, bool(force_matrix), method, bool(allow_single_cluster))
+           float(epsilon), precision, bool(force_matrix), method, bool(allow_single_cluster), str(input_dtype),
+           bool(normalize))
     with _plan_lock:
         plan = _plans.get(key)
         if plan is None:
             plan = Plan(offsets, dims, min_cluster_size=min_cluster_size, min_samples=min_samples,
                         cluster_selection_epsilon=epsilon, precision=precision, force_matrix=force_matrix,
-                        cluster_selection_method=method, allow_single_cluster=allow_single_cluster)
+                        cluster_selection_method=method, allow_single_cluster=allow_single_cluster,
+                        input_dtype=input_dtype, normalize=normalize)
             _plans[key] = plan
             if len(_plans) > 32:
                 _plans.popitem(last=False)
@@ -230,12 +238,15 @@ def plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, f
     return plan
 
 
-def to_device_tensor(X, precision) -> torch.Tensor:
-    """Native CUDA input stays on the device (cast/contiguous copy only); host input is uploaded."""
+def to_device_tensor(X, precision, keep_half=False) -> torch.Tensor:
+    """Native CUDA input stays on the device (cast/contiguous copy only); host input is uploaded.
+    keep_half: bfloat16/float16 tensors stay as they are (the producer stage converts them)."""
     torch_dtype, numpy_dtype, _ = _DTYPES[precision]
     if isinstance(X, torch.Tensor):
         if X.device.type != "cuda":
             X = X.to("cuda")
+        if keep_half and X.dtype in _HALF_INPUTS:
+            return X.contiguous()
         return X.to(torch_dtype).contiguous()
     if hasattr(X, "__dlpack__") and not isinstance(X, np.ndarray):
         return torch.from_dlpack(X).to(torch_dtype).contiguous()
@@ -244,10 +255,11 @@ def to_device_tensor(X, precision) -> torch.Tensor:
 
 
 def cluster(x, min_cluster_size, min_samples, epsilon, precision, method="eom", allow_single_cluster=False,
-            return_probabilities=False):
+            return_probabilities=False, normalize=False):
     """Labels for [N, D] or [B, N, D] input (the reference's backend seam)."""
     _require_gpu()
-    X = to_device_tensor(x, precision)
+    X = to_device_tensor(x, precision, keep_half=True)
+    input_dtype = X.dtype if X.dtype in _HALF_INPUTS else None
     with torch.cuda.device(X.device):
         unbatched = X.ndim == 2
         if unbatched:
@@ -255,7 +267,7 @@ def cluster(x, min_cluster_size, min_samples, epsilon, precision, method="eom", 
         batch, n, dims = X.shape
         offsets = np.arange(batch + 1, dtype=np.int64) * n
         plan = plan_for(offsets, dims, min_cluster_size, min_samples, epsilon, precision, method=method,
-                        allow_single_cluster=allow_single_cluster)
+                        allow_single_cluster=allow_single_cluster, input_dtype=input_dtype, normalize=normalize)
         exports = plan.export_buffers(hierarchy=False, probabilities=True) if return_probabilities else None
         labels, status = plan.forward(X.reshape(batch * n, dims), exports=exports)
         raise_for_status(int(status.item()))
@@ -267,9 +279,9 @@ def cluster(x, min_cluster_size, min_samples, epsilon, precision, method="eom", 
         return labels, (probs[0] if unbatched else probs)
 
 
-def pack(windows, precision="float32"):
+def pack(windows, precision="float32", keep_half=False):
     """Pack a list of [N_i, D] arrays/tensors into (packed [sum N, D] CUDA tensor, offsets int64)."""
-    tensors = [to_device_tensor(w, precision) for w in windows]
+    tensors = [to_device_tensor(w, precision, keep_half) for w in windows]
     if not tensors:
         raise ValueError("X requires nonempty batches/features and at least 2 samples")
     dims = {t.shape[-1] for t in tensors}
@@ -281,13 +293,15 @@ def pack(windows, precision="float32"):
 
 
 def cluster_ragged(packed, offsets, min_cluster_size, min_samples, epsilon, precision, exports=False,
-                   check=True, force_matrix=False, method="eom", allow_single_cluster=False):
+                   check=True, force_matrix=False, method="eom", allow_single_cluster=False, normalize=False):
     """Labels [sum N] for a ragged batch; optionally the hierarchy exports (with probabilities) too."""
     _require_gpu()
-    X = to_device_tensor(packed, precision)
+    X = to_device_tensor(packed, precision, keep_half=True)
+    input_dtype = X.dtype if X.dtype in _HALF_INPUTS else None
     with torch.cuda.device(X.device):
         plan = plan_for(offsets, X.shape[1], min_cluster_size, min_samples, epsilon, precision, force_matrix,
-                        method=method, allow_single_cluster=allow_single_cluster)
+                        method=method, allow_single_cluster=allow_single_cluster, input_dtype=input_dtype,
+                        normalize=normalize)
         buffers = plan.export_buffers(hierarchy=True, gradients=True, probabilities=True) if exports else None
         labels, status = plan.forward(X, exports=buffers)
         if check:

@@ -18,6 +18,9 @@ HDB_FLAG_NO_GRAPH_STREAMS = 2
 HDB_FLAG_ONE_PERSISTENT = 4
 HDB_FLAG_LEAF = 8
 HDB_FLAG_ALLOW_SINGLE = 16
+HDB_FLAG_INPUT_BF16 = 32
+HDB_FLAG_INPUT_F16 = 64
+HDB_FLAG_L2_NORMALIZE = 128
 STATUS_OVERFLOW = 1
 STATUS_NONFINITE = 2
 STATUS_INTERNAL = 4

@@ -9,7 +9,8 @@ from ._api import validate_limits, validate_parameters, validate_selection
 
 def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=5, min_samples=None,
                    cluster_selection_epsilon=0.0, precision="float32", return_hierarchy=False,
-                   force_matrix=False, cluster_selection_method="eom", allow_single_cluster=False):
+                   force_matrix=False, cluster_selection_method="eom", allow_single_cluster=False,
+                   normalize=False):
     """Cluster a ragged batch in one launch.
 
     Give either `windows` (a list of [N_i, D] arrays/tensors) or `packed`
@@ -27,11 +28,11 @@ def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=
     if windows is not None:
         if packed is not None or offsets is not None:
             raise ValueError("give either windows or packed+offsets")
-        packed, offsets = pack(windows, precision)
+        packed, offsets = pack(windows, precision, keep_half=True)
     else:
         if packed is None or offsets is None:
             raise ValueError("give either windows or packed+offsets")
-        packed = to_device_tensor(packed, precision)
+        packed = to_device_tensor(packed, precision, keep_half=True)
         offsets = np.asarray(offsets, dtype=np.int64)
     if packed.ndim != 2 or packed.shape[1] < 1:
         raise ValueError("X requires nonempty batches/features and at least 2 samples")
@@ -44,7 +45,7 @@ def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=
     result = cluster_ragged(packed, offsets, int(min_cluster_size), int(min_samples),
                             float(cluster_selection_epsilon), precision, exports=return_hierarchy,
                             force_matrix=force_matrix, method=cluster_selection_method,
-                            allow_single_cluster=allow_single_cluster)
+                            allow_single_cluster=allow_single_cluster, normalize=bool(normalize))
     if return_hierarchy:
         labels, exports = result
         return labels, offsets, exports

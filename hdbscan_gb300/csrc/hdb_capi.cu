@@ -90,7 +90,10 @@ struct hdb_plan {
     // Table layout (byte offsets within the workspace).
     size_t t_offsets = 0, t_dist_off = 0, t_queue = 0, t_tickets = 0, t_tiles = 0, t_edge_window = 0;
     size_t tables_bytes = 0;
-    size_t w_core = 0, w_core_nbr = 0, w_dist = 0, ws_bytes = 0;
+    size_t w_core = 0, w_core_nbr = 0, w_dist = 0, w_prep = 0, ws_bytes = 0;
+    int input_type = 0;     // hdb::InputType of X
+    int normalize = 0;      // L2-normalise every point first
+    bool prepared = false;  // X passes through the producer stage into the workspace
     unsigned char* h_tables = nullptr;      // pinned
     std::vector<cudaStream_t> aux;          // one per class (empty: everything on the caller's stream)
     std::vector<cudaEvent_t> events;        // [2i] class i inputs ready, [2i+1] class i done
@@ -431,6 +434,8 @@ int build_plan(hdb_plan* p) {
     if (!unit) ws += (size_t)p->T * sizeof(int32_t);
     p->w_dist = ws = align_up(ws, 256);
     ws += (size_t)p->dist_elems * rb;
+    p->w_prep = ws = align_up(ws, 256);
+    if (p->prepared) ws += (size_t)p->T * (size_t)p->D * rb;
     p->ws_bytes = align_up(std::max<size_t>(ws, 256), 256);
 
     // ---- streams for concurrent classes ------------------------------------
@@ -483,6 +488,11 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
     if (!ex) ex = &none;
     HDB_CUDA(cudaMemcpyAsync(ws, p->h_tables, p->tables_bytes, cudaMemcpyHostToDevice, stream));
     if (status) HDB_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), stream));
+    if (p->prepared) {  // producer stage: every later kernel reads the converted / normalised copy
+        HDB_CUDA(k.launch_prepare(X, p->input_type, ws + p->w_prep, p->T, p->D, p->normalize, stream,
+                                  p->classes.empty() ? 0 : p->classes[0].priority));
+        X = ws + p->w_prep;
+    }
     const int64_t* d_offsets = reinterpret_cast<const int64_t*>(ws + p->t_offsets);
     const int64_t* d_dist_off = reinterpret_cast<const int64_t*>(ws + p->t_dist_off);
     void* dist = ws + p->w_dist;
@@ -710,6 +720,13 @@ int hdb_plan_create(hdb_plan_t** out, int precision, int windows, const int64_t*
     p->eps = epsilon;
     p->flags = flags;
     p->offsets.assign(offsets_host, offsets_host + windows + 1);
+    if ((flags & HDB_FLAG_INPUT_BF16) && (flags & HDB_FLAG_INPUT_F16)) {
+        delete p;
+        return fail(HDB_E_INVALID, "X can be bfloat16 or float16, not both");
+    }
+    p->input_type = (flags & HDB_FLAG_INPUT_BF16) ? 1 : ((flags & HDB_FLAG_INPUT_F16) ? 2 : 0);
+    p->normalize = (flags & HDB_FLAG_L2_NORMALIZE) ? 1 : 0;
+    p->prepared = p->input_type != 0 || p->normalize != 0;
     p->T = offsets_host[windows];
     p->k = precision == HDB_F32 ? &hdb::kernels_f32() : &hdb::kernels_f64();
     cudaError_t e = cudaGetDevice(&p->device);
@@ -832,6 +849,8 @@ int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, con
     const bool unit = p->ms <= 2;
     if (!unit && (!ex->core || !ex->core_nbr))
         return fail(HDB_E_INVALID, "backward with min_samples > 2 needs the forward's core and core_nbr");
+    if (p->prepared)
+        return fail(HDB_E_INVALID, "backward needs input in the compute precision without normalisation");
     int rc = check_device(p);
     if (rc) return rc;
     rc = check_workspace(p, ws_v, ws_bytes);

@@ -5,6 +5,7 @@
 #include "hdb_distance.cuh"
 #include "hdb_forward.cuh"
 #include "hdb_launch.h"
+#include "hdb_prepare.cuh"
 #include "hdb_registry.h"
 
 namespace hdb {
@@ -57,6 +58,21 @@ cudaError_t launch_distance(const DistanceArgs& a, int grid, cudaStream_t s, int
 template <typename Real>
 cudaError_t launch_select(const CoreArgs& a, int grid, size_t smem, cudaStream_t s, int priority) {
     return launch_ex(hdb_core_select_kernel<Real>, grid, 256, smem, s, priority, 1, a);
+}
+
+template <typename Real>
+cudaError_t launch_prepare(const void* X, int input_type, void* out, int64_t points, int D, int normalize,
+                           cudaStream_t s, int priority) {
+    const unsigned grid = (unsigned)((points + 255) / 256);
+    Real* y = static_cast<Real*>(out);
+    if (input_type == kInputBF16)
+        return launch_ex(hdb_prepare_kernel<Real, __nv_bfloat16>, grid, 256, 0, s, priority, 1,
+                         static_cast<const __nv_bfloat16*>(X), y, points, D, normalize);
+    if (input_type == kInputF16)
+        return launch_ex(hdb_prepare_kernel<Real, __half>, grid, 256, 0, s, priority, 1, static_cast<const __half*>(X), y,
+                         points, D, normalize);
+    return launch_ex(hdb_prepare_kernel<Real, Real>, grid, 256, 0, s, priority, 1, static_cast<const Real*>(X), y,
+                     points, D, normalize);
 }
 
 template <typename Real>

@@ -55,7 +55,8 @@ const PrecisionKernels& kernels_f32() {
         PrecisionKernels t = {
             4, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), nullptr, 0, kCore,
             (int)(sizeof(kCore) / sizeof(kCore[0])), launch_distance<float>, launch_select<float>,
-            (const void*)hdb_core_select_kernel<float>, launch_backward<float>, forward_layout<float>,
+            (const void*)hdb_core_select_kernel<float>, launch_backward<float>, launch_prepare<float>,
+            forward_layout<float>,
         };
         t.cluster = cluster_variants_f32(&t.n_cluster);
         return t;

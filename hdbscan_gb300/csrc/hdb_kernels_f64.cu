@@ -42,7 +42,8 @@ const PrecisionKernels& kernels_f64() {
         PrecisionKernels t = {
             8, kForward, (int)(sizeof(kForward) / sizeof(kForward[0])), nullptr, 0, kCore,
             (int)(sizeof(kCore) / sizeof(kCore[0])), launch_distance<double>, launch_select<double>,
-            (const void*)hdb_core_select_kernel<double>, launch_backward<double>, forward_layout<double>,
+            (const void*)hdb_core_select_kernel<double>, launch_backward<double>, launch_prepare<double>,
+            forward_layout<double>,
         };
         t.cluster = cluster_variants_f64(&t.n_cluster);
         return t;

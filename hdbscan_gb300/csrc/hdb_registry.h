@@ -52,6 +52,9 @@ struct PrecisionKernels {
     cudaError_t (*launch_select)(const CoreArgs&, int grid, size_t smem, cudaStream_t, int priority);
     const void* select_func;
     cudaError_t (*launch_backward)(const BackwardArgs&, int grid, cudaStream_t, int priority);
+    // Producer stage: input (compute type / bfloat16 / float16) -> compute type, optionally L2-normalised.
+    cudaError_t (*launch_prepare)(const void* X, int input_type, void* out, int64_t points, int D, int normalize,
+                                  cudaStream_t, int priority);
     // Best single-CTA layout (at most max_arenas arenas) for windows of up to n
     // points within `budget` bytes; false if none fits.
     bool (*forward_layout)(int n, int dp, bool unit_core, size_t budget, int max_arenas, ForwardLayout* out);

@@ -63,6 +63,14 @@ extern "C" {
  * allow_single_cluster=) defines them (sklearn/cluster/_hdbscan/_tree.pyx). */
 #define HDB_FLAG_LEAF 8u           /* cluster_selection_method="leaf" */
 #define HDB_FLAG_ALLOW_SINGLE 16u  /* allow_single_cluster=True */
+/* Producer stage (no reference counterpart): X holds bfloat16 / float16
+ * values (converted exactly to the compute precision), and/or every point is
+ * L2-normalised first (s = sum of x_k*x_k in k order, x_k / sqrt(s), both
+ * round-to-nearest; zero vectors unchanged).  One pass into the workspace;
+ * hdb_plan_backward refuses such plans. */
+#define HDB_FLAG_INPUT_BF16 32u
+#define HDB_FLAG_INPUT_F16 64u
+#define HDB_FLAG_L2_NORMALIZE 128u
 
 typedef struct hdb_plan hdb_plan_t;
 

@@ -166,6 +166,23 @@ def cluster(x, min_cluster_size, min_samples=None, epsilon=0.0, precision="float
     return _trim(out, n)
 
 
+def normalize_rows(x, precision="float32"):
+    """The producer stage's L2 normalisation, restated: s = sum of x_k*x_k in
+    coordinate order, x_k / sqrt(s), every operation rounded to nearest in the
+    precision (NumPy scalar-type arithmetic, no fused multiply-add); zero
+    vectors unchanged."""
+    dtype, _ = _dtype(precision)
+    x = np.asarray(x, dtype=dtype)
+    s = np.zeros(x.shape[0], dtype)
+    for k in range(x.shape[1]):
+        s = s + x[:, k] * x[:, k]
+    r = np.sqrt(s)
+    out = x.copy()
+    nz = r > 0
+    out[nz] = x[nz] / r[nz, None]
+    return out
+
+
 def graph(distances, core, min_cluster_size, epsilon=0.0, precision=None):
     """Hierarchy and labels from a caller-supplied distance matrix; core None = unit core."""
     distances = np.asarray(distances)
