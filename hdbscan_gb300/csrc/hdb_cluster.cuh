@@ -390,19 +390,19 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
             } else {
                 const Real* __restrict__ row = Dw + (int64_t)cur * ld;
 #pragma unroll
-                for (int v = 0; v < SV; ++v) acc[v] = act[v] ? __ldcg(row + vid[v]) : Real(0);
+                for (int v = 0; v < SV; ++v) acc[v] = __ldcg(row + (act[v] ? vid[v] : 0));
             }
             Key lkey = SENTINEL;
             uint32_t lidx = 0xffffffffu;
 #pragma unroll
             for (int v = 0; v < SV; ++v) {
                 if constexpr (DP > 0) {
-                    acc_max = act[v] ? T::maxr(acc_max, acc[v]) : acc_max;
-                    const Real cm = UNIT ? Real(0) : T::maxr(core_cur, core_r[v]);
-                    if (act[v] && acc[v] < thr[v] && (UNIT || cm < best[v])) {
+                    acc_max = T::sel(act[v], T::vmax(acc_max, acc[v]), acc_max);
+                    const Real cm = UNIT ? Real(0) : T::vmax(core_cur, core_r[v]);
+                    if (act[v] && T::lt(acc[v], thr[v]) && (UNIT || T::lt(cm, best[v]))) {
                         const Real d = T::sqrt_rn(acc[v]);
-                        const Real wgt = UNIT ? d : T::maxr(cm, d);
-                        if (wgt < best[v]) {  // strict: equal weights keep the older source
+                        const Real wgt = UNIT ? d : T::vmax(cm, d);
+                        if (T::lt(wgt, best[v])) {  // strict: equal weights keep the older source
                             best[v] = wgt;
                             src[v] = cur;
                             thr[v] = T::mul_ru(wgt, wgt);
@@ -411,14 +411,14 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
                 } else {
                     if (act[v]) {
                         const Real d = acc[v];
-                        overflow |= (d <= T::kMax) ? 0 : 2;
-                        const Real wgt = UNIT ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
-                        if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
+                        overflow |= T::finite_nn(d) ? 0 : 2;
+                        const Real wgt = UNIT ? d : T::vmax(T::vmax(core_cur, core_r[v]), d);
+                        if (T::lt(wgt, best[v])) { best[v] = wgt; src[v] = cur; }
                     }
                 }
                 const Key key = act[v] ? T::key(best[v]) : SENTINEL;
                 const uint32_t j = (uint32_t)vid[v];
-                if (key < lkey || (key == lkey && j < lidx)) { lkey = key; lidx = j; }
+                if (key_idx_lt(key, j, lkey, lidx)) { lkey = key; lidx = j; }
             }
             warp_argmin(lkey, lidx);
             const int buf = it & 1;
@@ -432,7 +432,7 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
             const uint32_t p = xc & 1, ph = (xc >> 1) & 1;
             ++xc;
             const uint32_t slot = cs.recs + (p * CS + rank) * Rec::kBytes;
-            if (gk != SENTINEL) {
+            if (!key_eq(gk, SENTINEL)) {
 #pragma unroll
                 for (int v = 0; v < SV; ++v) {
                     if (act[v] && vid[v] == (int)gi) {
@@ -453,10 +453,10 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
                 const unsigned char* rp = cs.recs_ptr + (p * CS + r) * Rec::kBytes;
                 const Key k = *reinterpret_cast<const Key*>(rp);
                 const uint32_t vs = *reinterpret_cast<const uint32_t*>(rp + sizeof(Key));
-                if (k < wk || (k == wk && (vs & 0xffffu) < (wv & 0xffffu))) { wk = k; wv = vs; wr = r; }
+                if (key_idx_lt(k, vs & 0xffffu, wk, wv & 0xffffu)) { wk = k; wv = vs; wr = r; }
             }
             int next = (int)(wv & 0xffffu);
-            if (wk == SENTINEL || next >= n) {  // unreachable: a non-tree vertex always remains
+            if (key_eq(wk, SENTINEL) || next >= n) {  // unreachable: a non-tree vertex always remains
                 overflow |= 4;
                 next = 0;
             }

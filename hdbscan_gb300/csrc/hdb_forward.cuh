@@ -230,10 +230,11 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
                     }
             }
         } else {
-            // Matrix variant: row `cur` of the window's distance block.
+            // Matrix variant: row `cur` of the window's distance block (slots
+            // outside the tree set read entry 0 and ignore it).
             const Real* __restrict__ row = Dw + (int64_t)cur * (int64_t)((n + 3) & ~3);
 #pragma unroll
-            for (int v = 0; v < SV; ++v) acc[v] = act[v] ? __ldcg(row + vid[v]) : Real(0);
+            for (int v = 0; v < SV; ++v) acc[v] = __ldcg(row + (act[v] ? vid[v] : 0));
         }
         Key lkey = SENTINEL;
         uint32_t lidx = 0xffffffffu;
@@ -242,12 +243,12 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
             if constexpr (DP > 0) {
                 // sqrt_rn is monotone and best representable: acc >= RU(best^2)
                 // gives sqrt_rn(acc) >= best, so no strict improvement.
-                acc_max = act[v] ? T::maxr(acc_max, acc[v]) : acc_max;
-                const Real cm = UNIT ? Real(0) : T::maxr(core_cur, core_r[v]);
-                if (act[v] && acc[v] < thr[v] && (UNIT || cm < best[v])) {
+                acc_max = T::sel(act[v], T::vmax(acc_max, acc[v]), acc_max);
+                const Real cm = UNIT ? Real(0) : T::vmax(core_cur, core_r[v]);
+                if (act[v] && T::lt(acc[v], thr[v]) && (UNIT || T::lt(cm, best[v]))) {
                     const Real d = T::sqrt_rn(acc[v]);
-                    const Real wgt = UNIT ? d : T::maxr(cm, d);
-                    if (wgt < best[v]) {  // strict: equal weights keep the older source
+                    const Real wgt = UNIT ? d : T::vmax(cm, d);
+                    if (T::lt(wgt, best[v])) {  // strict: equal weights keep the older source
                         best[v] = wgt;
                         src[v] = cur;
                         thr[v] = T::mul_ru(wgt, wgt);
@@ -256,14 +257,14 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
             } else {
                 if (act[v]) {
                     const Real d = acc[v];
-                    overflow |= !(d <= T::kMax);
-                    const Real wgt = UNIT ? d : T::maxr(T::maxr(core_cur, core_r[v]), d);
-                    if (wgt < best[v]) { best[v] = wgt; src[v] = cur; }
+                    overflow |= !T::finite_nn(d);
+                    const Real wgt = UNIT ? d : T::vmax(T::vmax(core_cur, core_r[v]), d);
+                    if (T::lt(wgt, best[v])) { best[v] = wgt; src[v] = cur; }
                 }
             }
             const Key key = act[v] ? T::key(best[v]) : SENTINEL;
             const uint32_t j = (uint32_t)vid[v];
-            if (key < lkey || (key == lkey && j < lidx)) { lkey = key; lidx = j; }
+            if (key_idx_lt(key, j, lkey, lidx)) { lkey = key; lidx = j; }
         }
         warp_argmin(lkey, lidx);
         const int buf = it & 1;

@@ -15,14 +15,16 @@
 //    right (and symmetrically for B), and stops at i = min(A[K], B[K-1]) for
 //    K swaps.  Ranks come from ballots, so each partition is two passes over
 //    the segment plus K/32 swap rounds, with NumPy's exact swap sequence.
-//    Segments of <= 16 elements and depth-exhausted heapsort segments are
-//    finished one per lane.
+//    Segments shorter than a threshold (m/16 clamped to [32, 128]) and
+//    depth-exhausted heapsort segments are finished one per lane by the
+//    serial algorithm itself (partitions, stack, insertion sort, heapsort);
+//    segments are disjoint, so the order in which they finish is irrelevant;
 //  * windows whose edge weights are all distinct are sorted by a stable warp
 //    LSD radix sort instead (the argsort of distinct keys is unique, so it
 //    equals NumPy's); a window with any tied weight falls back to the exact
 //    introsort above;
-//  * linkage uses union by size over packed 64-bit words
-//    (parent | component node << 16 | size << 32) without path compression;
+//  * linkage uses union by size over packed 32-bit word pairs
+//    {parent | component node << 16, size} without path compression;
 //    the roots, hence the tree, are those of the reference's union-find.
 //  * condensation runs the reference's breadth-first queue one level at a
 //    time across the warp: every cluster is a path of the dendrogram (it only
@@ -100,8 +102,8 @@ __device__ void heap_sort_pairs(SortPair<Real>* p, int lo, int hi) {
         SortPair<Real> value = a[root];
         int pos = root, child = 2 * root;
         while (child <= count) {
-            if (child < count && a[child].w < a[child + 1].w) ++child;
-            if (value.w < a[child].w) { a[pos] = a[child]; pos = child; child *= 2; } else break;
+            if (child < count && RealTraits<Real>::lt(a[child].w, a[child + 1].w)) ++child;
+            if (RealTraits<Real>::lt(value.w, a[child].w)) { a[pos] = a[child]; pos = child; child *= 2; } else break;
         }
         a[pos] = value;
     }
@@ -111,8 +113,8 @@ __device__ void heap_sort_pairs(SortPair<Real>* p, int lo, int hi) {
         --end;
         int pos = 1, child = 2;
         while (child <= end) {
-            if (child < end && a[child].w < a[child + 1].w) ++child;
-            if (value.w < a[child].w) { a[pos] = a[child]; pos = child; child *= 2; } else break;
+            if (child < end && RealTraits<Real>::lt(a[child].w, a[child + 1].w)) ++child;
+            if (RealTraits<Real>::lt(value.w, a[child].w)) { a[pos] = a[child]; pos = child; child *= 2; } else break;
         }
         a[pos] = value;
     }
@@ -123,7 +125,7 @@ __device__ void insertion_sort_pairs(SortPair<Real>* p, int lo, int hi) {
     for (int i = lo + 1; i <= hi; ++i) {
         SortPair<Real> value = p[i];
         int j = i;
-        while (j > lo && value.w < p[j - 1].w) { p[j] = p[j - 1]; --j; }
+        while (j > lo && RealTraits<Real>::lt(value.w, p[j - 1].w)) { p[j] = p[j - 1]; --j; }
         p[j] = value;
     }
 }
@@ -133,6 +135,65 @@ __device__ __forceinline__ void swap_pairs(SortPair<Real>* p, int i, int j) {
     SortPair<Real> t = p[i]; p[i] = p[j]; p[j] = t;
 }
 
+// One Hoare partition of p[lo..hi] (hi - lo > 15) by one lane: NumPy's
+// median-of-three, pivot parked at hi-1, unguarded i/j scans (p[hi-1] and
+// p[lo] are the sentinels) and the final swap (_kernels.py:444-462).
+template <typename Real>
+__device__ int partition_serial(SortPair<Real>* p, int lo, int hi) {
+    const int mid = lo + ((hi - lo) >> 1);
+    if (RealTraits<Real>::lt(p[mid].w, p[lo].w)) swap_pairs(p, mid, lo);
+    if (RealTraits<Real>::lt(p[hi].w, p[mid].w)) swap_pairs(p, hi, mid);
+    if (RealTraits<Real>::lt(p[mid].w, p[lo].w)) swap_pairs(p, mid, lo);
+    swap_pairs(p, mid, hi - 1);
+    const Real pivot = p[hi - 1].w;
+    int i = lo, j = hi - 1;
+    for (;;) {
+        do ++i; while (RealTraits<Real>::lt(p[i].w, pivot));
+        do --j; while (RealTraits<Real>::lt(pivot, p[j].w));
+        if (i >= j) break;
+        swap_pairs(p, i, j);
+    }
+    swap_pairs(p, i, hi - 1);
+    return i;
+}
+
+// Segments shorter than this many elements (or depth-exhausted) are sorted by
+// one lane.  The lane's stack holds the larger sides while the loop continues
+// on the smaller one, so a segment of s elements never stacks more than
+// log2(s/16) + 1 entries.
+constexpr int kLaneSortMax = 128;
+constexpr int kLaneStack = 8;
+static_assert((kLaneSortMax >> (kLaneStack - 1)) <= 16, "lane introsort stack too small");
+
+// NumPy's aquicksort loop on one segment by one lane.  code = depth*2 +
+// checked: a checked segment with negative depth is heapsorted (the check a
+// popped segment gets); an unchecked one (the smaller side that the loop
+// continues on) is partitioned first (_kernels.py:433-470).
+template <typename Real>
+__device__ void introsort_lane(SortPair<Real>* p, int lo, int hi, int code) {
+    int depth = code >> 1;  // arithmetic shift keeps negative depths
+    bool checked = code & 1;
+    int st_lo[kLaneStack], st_hi[kLaneStack], st_depth[kLaneStack];
+    int top = 0;
+    for (;;) {
+        if (checked && depth < 0) {
+            heap_sort_pairs(p, lo, hi);
+        } else {
+            while (hi - lo > 15) {
+                const int i = partition_serial(p, lo, hi);
+                --depth;
+                if (i - lo < hi - i) { st_lo[top] = i + 1; st_hi[top] = hi; hi = i - 1; }
+                else { st_lo[top] = lo; st_hi[top] = i - 1; lo = i + 1; }
+                st_depth[top++] = depth;
+            }
+            insertion_sort_pairs(p, lo, hi);
+        }
+        if (top == 0) return;
+        --top;
+        lo = st_lo[top]; hi = st_hi[top]; depth = st_depth[top]; checked = true;
+    }
+}
+
 // One Hoare partition of p[lo..hi] (hi - lo > 15) by the whole warp.
 // Returns the pivot's final position (warp-uniform).
 template <typename Real>
@@ -140,9 +201,9 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         const int mid = lo + ((hi - lo) >> 1);
-        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
-        if (p[hi].w < p[mid].w) swap_pairs(p, hi, mid);
-        if (p[mid].w < p[lo].w) swap_pairs(p, mid, lo);
+        if (RealTraits<Real>::lt(p[mid].w, p[lo].w)) swap_pairs(p, mid, lo);
+        if (RealTraits<Real>::lt(p[hi].w, p[mid].w)) swap_pairs(p, hi, mid);
+        if (RealTraits<Real>::lt(p[mid].w, p[lo].w)) swap_pairs(p, mid, lo);
         swap_pairs(p, mid, hi - 1);
     }
     __syncwarp();
@@ -154,8 +215,8 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
         bool fa = false, fb = false;
         if (pos <= hi - 1) {
             const Real w = p[pos].w;
-            fa = pos >= lo + 1 && !(w < pivot);
-            fb = pos <= hi - 2 && !(pivot < w);
+            fa = pos >= lo + 1 && !RealTraits<Real>::lt(w, pivot);
+            fb = pos <= hi - 2 && !RealTraits<Real>::lt(pivot, w);
         }
         total_a += __popc(__ballot_sync(0xffffffffu, fa));
         total_b += __popc(__ballot_sync(0xffffffffu, fb));
@@ -168,8 +229,8 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
         bool fa = false, fb = false;
         if (pos <= hi - 1) {
             const Real w = p[pos].w;
-            fa = pos >= lo + 1 && !(w < pivot);
-            fb = pos <= hi - 2 && !(pivot < w);
+            fa = pos >= lo + 1 && !RealTraits<Real>::lt(w, pivot);
+            fb = pos <= hi - 2 && !RealTraits<Real>::lt(pivot, w);
         }
         const unsigned ba = __ballot_sync(0xffffffffu, fa);
         const unsigned bb = __ballot_sync(0xffffffffu, fb);
@@ -199,6 +260,12 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
     return i;
 }
 
+__device__ __forceinline__ int radix_digit(uint32_t k, int shift) { return (int)((k >> shift) & 0xffu); }
+__device__ __forceinline__ int radix_digit(unsigned long long k, int shift) {
+    const uint32_t w = shift < 32 ? (uint32_t)k : (uint32_t)(k >> 32);
+    return (int)((w >> (shift & 31)) & 0xffu);
+}
+
 // Stable LSD radix sort (8-bit digits) of the order-preserving keys of
 // r0[0..m) with their indices, by one warp.  Returns false, leaving r0 intact,
 // when two keys are equal; otherwise writes the order to s2 and the sorted
@@ -224,7 +291,7 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
         __syncwarp();
         for (int base = 0; base < m; base += 32) {
             const int i = base + lane;
-            const int d = i < m ? (int)((kin[i] >> shift) & 0xff) : 256;
+            const int d = i < m ? radix_digit(kin[i], shift) : 256;
             const unsigned same = __match_any_sync(0xffffffffu, d);
             if (d < 256 && (same & lt) == 0) hist[d] += __popc(same);
             __syncwarp();
@@ -248,7 +315,7 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
             const int i = base + lane;
             const bool valid = i < m;
             const Key k = valid ? kin[i] : Key(0);
-            const int d = valid ? (int)((k >> shift) & 0xff) : 256;
+            const int d = valid ? radix_digit(k, shift) : 256;
             const unsigned same = __match_any_sync(0xffffffffu, d);
             int pos = 0;
             if (valid) pos = hist[d] + __popc(same & lt);
@@ -265,7 +332,7 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
         __syncwarp();
     }
     bool dup = false;
-    for (int i = lane; i + 1 < m; i += 32) dup |= kin[i] == kin[i + 1];
+    for (int i = lane; i + 1 < m; i += 32) dup |= key_eq(kin[i], kin[i + 1]);
     if (__any_sync(0xffffffffu, dup)) return false;
     for (int i = lane; i < m; i += 32) {
         a.s2[i] = iin[i];
@@ -285,7 +352,10 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
     SortPair<Real>* p = reinterpret_cast<SortPair<Real>*>(a.r1);
     for (int i = lane; i < m; i += 32) { p[i].w = a.r0[i]; p[i].idx = i; }
     int16_t *task_lo = a.s5, *task_hi = a.s6, *task_depth = a.s7;  // depth*2 + checked
-    int16_t *leaf_lo = a.s8, *leaf_hi = a.s9;                        // hi < 0: heapsort ~hi
+    int16_t *leaf_lo = a.s8, *leaf_hi = a.s9, *leaf_code = a.s2;     // segments finished by lanes
+    // Warp partitions down to about m/16 elements leave some 16-32 segments
+    // for the lanes.
+    const int lane_max = min(kLaneSortMax, max(32, m >> 4));
     int top = 0, leaves = 0;
     if (m > 1) {
         int depth = 0;
@@ -300,12 +370,9 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
         const int depth = code >> 1;  // arithmetic shift keeps negative depths
         const bool checked = code & 1;
         __syncwarp();
-        if (checked && depth < 0) {
-            // Popped task with exhausted depth: heapsort (reference :442-443).
-            if (lane == 0) { leaf_lo[leaves] = (int16_t)lo; leaf_hi[leaves] = (int16_t)~hi; }
-            ++leaves;
-        } else if (hi - lo <= 15) {
-            if (lane == 0) { leaf_lo[leaves] = (int16_t)lo; leaf_hi[leaves] = (int16_t)hi; }
+        if ((checked && depth < 0) || hi - lo + 1 < lane_max) {
+            // Exhausted depth (heapsort, reference :442-443) or a short segment.
+            if (lane == 0) { leaf_lo[leaves] = (int16_t)lo; leaf_hi[leaves] = (int16_t)hi; leaf_code[leaves] = (int16_t)code; }
             ++leaves;
         } else {
             const int i = partition_warp(p, lo, hi, a.s3, a.s4);
@@ -324,11 +391,7 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
         }
         __syncwarp();
     }
-    for (int t = lane; t < leaves; t += 32) {
-        const int lo = leaf_lo[t], hi = leaf_hi[t];
-        if (hi < 0) heap_sort_pairs(p, lo, ~hi);
-        else insertion_sort_pairs(p, lo, hi);
-    }
+    for (int t = lane; t < leaves; t += 32) introsort_lane(p, leaf_lo[t], leaf_hi[t], leaf_code[t]);
     __syncwarp();
     for (int i = lane; i < m; i += 32) {
         a.s2[i] = (int16_t)p[i].idx;
@@ -346,29 +409,28 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
 template <typename Real>
 __device__ void linkage_warp(const Arena<Real>& a, int n) {
     const int lane = threadIdx.x & 31;
-    unsigned long long* U = reinterpret_cast<unsigned long long*>(a.r1);
-    for (int x = lane; x < n; x += 32)
-        U[x] = (unsigned long long)x | ((unsigned long long)x << 16) | (1ull << 32);
+    uint2* U = reinterpret_cast<uint2*>(a.r1);  // {parent | node << 16, size}
+    for (int x = lane; x < n; x += 32) U[x] = make_uint2((uint32_t)x | ((uint32_t)x << 16), 1u);
     __syncwarp();
     if (lane == 0) {
         int xn = a.s2[0], yn = a.s3[0];  // n >= 2: at least one edge
         for (int i = 0; i < n - 1; ++i) {
             int x = xn, y = yn;
             if (i + 2 < n) { xn = a.s2[i + 1]; yn = a.s3[i + 1]; }  // next endpoints, off the critical path
-            unsigned long long wx = U[x], wy = U[y];
-            while ((int)(wx & 0xffff) != x) { x = (int)(wx & 0xffff); wx = U[x]; }
-            while ((int)(wy & 0xffff) != y) { y = (int)(wy & 0xffff); wy = U[y]; }
-            const unsigned long long sx = wx >> 32, sy = wy >> 32, s = sx + sy;
-            a.s4[i] = (int16_t)((wx >> 16) & 0xffff);
-            a.s5[i] = (int16_t)((wy >> 16) & 0xffff);
+            uint2 wx = U[x], wy = U[y];
+            while ((int)(wx.x & 0xffffu) != x) { x = (int)(wx.x & 0xffffu); wx = U[x]; }
+            while ((int)(wy.x & 0xffffu) != y) { y = (int)(wy.x & 0xffffu); wy = U[y]; }
+            const uint32_t sx = wx.y, sy = wy.y, s = sx + sy;
+            a.s4[i] = (int16_t)(wx.x >> 16);
+            a.s5[i] = (int16_t)(wy.x >> 16);
             a.s6[i] = (int16_t)s;
-            const unsigned long long node = (unsigned long long)(n + i) << 16;
+            const uint32_t node = (uint32_t)(n + i) << 16;
             if (sx < sy) {
-                U[x] = (wx & ~0xffffull) | (unsigned long long)y;
-                U[y] = (unsigned long long)y | node | (s << 32);
+                U[x].x = (wx.x & 0xffff0000u) | (uint32_t)y;
+                U[y] = make_uint2((uint32_t)y | node, s);
             } else {
-                U[y] = (wy & ~0xffffull) | (unsigned long long)x;
-                U[x] = (unsigned long long)x | node | (s << 32);
+                U[y].x = (wy.x & 0xffff0000u) | (uint32_t)x;
+                U[x] = make_uint2((uint32_t)x | node, s);
             }
         }
     }
