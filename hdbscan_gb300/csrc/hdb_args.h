@@ -56,6 +56,7 @@ struct DistanceArgs {
     const int64_t* offsets;
     const int32_t* tiles;        // [n_tiles, 3] = (window, tile row, tile col), col >= row
     int n_tiles;
+    int tile;                    // tile edge: 64, or 128 (float32 only)
     int D;
     void* dist;                  // packed blocks
     const int64_t* dist_offsets; // [B]

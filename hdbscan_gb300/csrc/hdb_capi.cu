@@ -65,6 +65,7 @@ struct WindowClass {
     int priority = 0;          // launch priority (largest windows highest)
     size_t tiles_first = 0;    // first distance tile (triple) of this class
     size_t n_tiles = 0;
+    int tile = 64;             // distance tile edge
     std::vector<CoreLaunch> cores;
 };
 
@@ -125,6 +126,7 @@ int real_bytes(int precision) { return precision == HDB_F32 ? 4 : 8; }
 
 constexpr size_t kChunks = 4;     // pipeline depth for large matrix-variant classes
 constexpr size_t kMinChunk = 8;   // windows per chunk at least
+constexpr int kTile128MinN = 384;  // float32 matrix classes from this size use 128x128 distance tiles
 
 cudaError_t raise_smem_limit(const void* func, size_t bytes) { return hdb::raise_dynamic_smem(func, bytes); }
 
@@ -316,12 +318,14 @@ int build_plan(hdb_plan* p) {
     for (auto& c : p->classes) {
         c.tiles_first = p->tiles.size() / 3;
         if (c.fv->dp != 0) continue;
+        // Float32 classes of larger windows take the 128x128 tile kernel.
+        c.tile = (p->precision == HDB_F32 && c.nmax >= kTile128MinN) ? 128 : 64;
         for (int w : c.windows) {
             const int n = size_of(w);
             const int64_t ld = (n + 3) & ~3;
             p->dist_offsets[w] = p->dist_elems;
             p->dist_elems += align_up((size_t)(n * ld), 64);
-            const int t = (n + 63) / 64;
+            const int t = (n + c.tile - 1) / c.tile;
             for (int ti = 0; ti < t; ++ti)
                 for (int tj = ti; tj < t; ++tj) {
                     p->tiles.push_back(w);
@@ -514,6 +518,7 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
             a.offsets = d_offsets;
             a.tiles = reinterpret_cast<const int32_t*>(ws + p->t_tiles) + 3 * c.tiles_first;
             a.n_tiles = (int)c.n_tiles;
+            a.tile = c.tile;
             a.D = p->D;
             a.dist = dist;
             a.dist_offsets = d_dist_off;
@@ -769,7 +774,8 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
              ",\"per_sm\":" + std::to_string(c.fv->per_sm) +
              ",\"variant\":\"" + (c.fv->dp ? "recompute" : "matrix") +
              "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
-             ",\"distance_tiles\":" + std::to_string(c.n_tiles) + ",\"priority\":" + std::to_string(c.priority) +
+             ",\"distance_tiles\":" + std::to_string(c.n_tiles) + ",\"tile\":" + std::to_string(c.tile) +
+             ",\"priority\":" + std::to_string(c.priority) +
              ",\"windows\":" +
              std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
              std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";

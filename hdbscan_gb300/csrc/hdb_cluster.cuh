@@ -380,12 +380,27 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
                         c[0] = q.x; c[1 % VEC] = q.y;
                     }
 #pragma unroll
-                    for (int v = 0; v < SV; ++v)
+                    for (int v = 0; v < SV; ++v) {
+                        if constexpr (sizeof(Real) == 4) {
+                            // Packed differences (fma(c, -1, x) = RN(x - c)) and
+                            // squares; scalar k-ordered sum, as in hdb_forward.cuh.
 #pragma unroll
-                        for (int kk = 0; kk < VEC; ++kk) {
-                            const Real delta = T::sub(c[kk], xr[v][k0 + kk]);
-                            acc[v] = T::add(acc[v], T::mul(delta, delta));
+                            for (int kk = 0; kk < VEC; kk += 2) {
+                                const float2 delta =
+                                    __ffma2_rn(make_float2(c[kk], c[kk + 1]), make_float2(-1.0f, -1.0f),
+                                               make_float2(xr[v][k0 + kk], xr[v][k0 + kk + 1]));
+                                const float2 sq = __fmul2_rn(delta, delta);
+                                acc[v] = T::add(acc[v], sq.x);
+                                acc[v] = T::add(acc[v], sq.y);
+                            }
+                        } else {
+#pragma unroll
+                            for (int kk = 0; kk < VEC; ++kk) {
+                                const Real delta = T::sub(c[kk], xr[v][k0 + kk]);
+                                acc[v] = T::add(acc[v], T::mul(delta, delta));
+                            }
                         }
+                    }
                 }
             } else {
                 const Real* __restrict__ row = Dw + (int64_t)cur * ld;

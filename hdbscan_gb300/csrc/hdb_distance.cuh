@@ -101,22 +101,50 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
         // staged coordinate keeps all squares normal, else the hardware multiply.
         const bool int_square = __syncthreads_and(safe);
         const int kend = min(KC, D - k0);
-        auto accumulate = [&](auto square) {
-            for (int k = 0; k < kend; ++k) {
-                Real xi[4], xj[4];
-                DistVec<Real>::load4(&s_i[k][ty * 4], xi);
-                DistVec<Real>::load4(&s_j[k][tx * 4], xj);
+        if constexpr (sizeof(Real) == 4) {
+            // Packed differences and squares (x_i - x_j = fma(x_j, -1, x_i),
+            // exact product and one rounding), scalar k-ordered sums.  Full
+            // chunks run unrolled so the shared loads of later k issue early.
+            auto step = [&](int k) {
+                float xi[4], xj[4];
+                DistVec<float>::load4(&s_i[k][ty * 4], xi);
+                DistVec<float>::load4(&s_j[k][tx * 4], xj);
 #pragma unroll
-                for (int a = 0; a < 4; ++a)
+                for (int a = 0; a < 4; ++a) {
+                    const float2 xa = make_float2(xi[a], xi[a]);
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) {
-                        const Real delta = T::sub(xi[a], xj[b]);
-                        acc[a][b] = T::add(acc[a][b], square(delta));
+                    for (int b = 0; b < 4; b += 2) {
+                        const float2 d = __ffma2_rn(make_float2(xj[b], xj[b + 1]), make_float2(-1.0f, -1.0f), xa);
+                        const float2 q = __fmul2_rn(d, d);
+                        acc[a][b] = T::add(acc[a][b], q.x);
+                        acc[a][b + 1] = T::add(acc[a][b + 1], q.y);
                     }
+                }
+            };
+            if (kend == KC) {
+#pragma unroll 8
+                for (int k = 0; k < KC; ++k) step(k);
+            } else {
+                for (int k = 0; k < kend; ++k) step(k);
             }
-        };
-        if (sizeof(Real) == 8 && int_square) accumulate([](Real d) { return T::sqr(d); });
-        else accumulate([](Real d) { return T::mul(d, d); });
+        } else {
+            auto accumulate = [&](auto square) {
+                for (int k = 0; k < kend; ++k) {
+                    Real xi[4], xj[4];
+                    DistVec<Real>::load4(&s_i[k][ty * 4], xi);
+                    DistVec<Real>::load4(&s_j[k][tx * 4], xj);
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const Real delta = T::sub(xi[a], xj[b]);
+                            acc[a][b] = T::add(acc[a][b], square(delta));
+                        }
+                }
+            };
+            if (int_square) accumulate([](Real d) { return T::sqr(d); });
+            else accumulate([](Real d) { return T::mul(d, d); });
+        }
         __syncthreads();
     }
     int overflow = 0;
@@ -149,25 +177,159 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
     if (__syncthreads_or(overflow) && tid == 0) atomic_status(args.status, kOverflow);
 }
 
+// Float32 blocks of larger windows: 128x128 tiles, 256 threads, 8x8 pairs per
+// thread (rows ty*4..+3 and 64+ty*4..+3, columns likewise from tx), so every
+// shared load feeds 16 pair updates and the accumulators give 64-way
+// independence.  Per pair the arithmetic is that of hdb_distance_kernel: the
+// difference x_i - x_j as fma(x_j, -1, x_i) (exact product, one rounding) and
+// its square in packed f32x2 instructions, the k-ordered sum in scalar
+// round-to-nearest adds, a correctly rounded sqrt.
+constexpr int kDistTile128 = 128;
+
+template <typename Real>
+__global__ void __launch_bounds__(256, 2) hdb_distance128_kernel(const DistanceArgs args) {
+    static_assert(sizeof(Real) == 4, "the 128x128 tile kernel is float32 only");
+    using T = RealTraits<float>;
+    constexpr int KC = 32;
+    constexpr int TS = kDistTile128;
+    __shared__ __align__(16) float s_i[KC][TS];
+    __shared__ __align__(16) float s_j[KC][TS];
+    const int tile = blockIdx.x;
+    if (tile >= args.n_tiles) return;
+    const int w = args.tiles[3 * tile], ti = args.tiles[3 * tile + 1], tj = args.tiles[3 * tile + 2];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const int D = args.D;
+    const float* __restrict__ Xw = static_cast<const float*>(args.X) + base * D;
+    float* __restrict__ Dw = static_cast<float*>(args.dist) + args.dist_offsets[w];
+    const int64_t ld = dist_ld(n);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int i0 = ti * TS, j0 = tj * TS;
+
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.0f;
+
+    for (int k0 = 0; k0 < D; k0 += KC) {
+        // Stage [128 rows x KC coords] of each block transposed to [KC][128]:
+        // lanes walk the row index (conflict-free stores); each thread covers
+        // KC/2 coordinates of one row.
+        {
+            const int r = tid & (TS - 1), kq = tid >> 7;
+            const int gi = i0 + r, gj = j0 + r;
+#pragma unroll
+            for (int kk = 0; kk < KC / 2; ++kk) {
+                const int k = kq * (KC / 2) + kk, gk = k0 + k;
+                s_i[k][r] = (gi < n && gk < D) ? Xw[(int64_t)gi * D + gk] : 0.0f;
+                s_j[k][r] = (gj < n && gk < D) ? Xw[(int64_t)gj * D + gk] : 0.0f;
+            }
+        }
+        __syncthreads();
+        const int kend = min(KC, D - k0);
+        auto step = [&](int k) {
+            float xi[8], xj[8];
+            DistVec<float>::load4(&s_i[k][ty * 4], xi);
+            DistVec<float>::load4(&s_i[k][64 + ty * 4], xi + 4);
+            DistVec<float>::load4(&s_j[k][tx * 4], xj);
+            DistVec<float>::load4(&s_j[k][64 + tx * 4], xj + 4);
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const float2 xa = make_float2(xi[a], xi[a]);
+#pragma unroll
+                for (int b = 0; b < 8; b += 2) {
+                    const float2 d = __ffma2_rn(make_float2(xj[b], xj[b + 1]), make_float2(-1.0f, -1.0f), xa);
+                    const float2 q = __fmul2_rn(d, d);
+                    acc[a][b] = T::add(acc[a][b], q.x);
+                    acc[a][b + 1] = T::add(acc[a][b + 1], q.y);
+                }
+            }
+        };
+        if (kend == KC) {
+#pragma unroll 4
+            for (int k = 0; k < KC; ++k) step(k);
+        } else {
+            for (int k = 0; k < kend; ++k) step(k);
+        }
+        __syncthreads();
+    }
+    int overflow = 0;
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            acc[a][b] = T::sqrt_rn(acc[a][b]);
+            const int gi = i0 + (a < 4 ? ty * 4 + a : 64 + ty * 4 + a - 4);
+            const int gj = j0 + (b < 4 ? tx * 4 + b : 64 + tx * 4 + b - 4);
+            if (gi < n && gj < n) overflow |= !(acc[a][b] <= T::kMax);
+        }
+    // Direct block: row gi, columns cj..cj+3 (ld is a multiple of 4, so a
+    // column group that starts below ld ends below it).
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int cj = j0 + h * 64 + tx * 4;
+        if (cj < ld) {
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const int gi = i0 + (a < 4 ? ty * 4 + a : 64 + ty * 4 + a - 4);
+                if (gi < n)
+                    DistVec<float>::store4(Dw + gi * ld + cj, acc[a][4 * h], acc[a][4 * h + 1], acc[a][4 * h + 2],
+                                           acc[a][4 * h + 3]);
+            }
+        }
+    }
+    if (ti != tj) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int ci = i0 + h * 64 + ty * 4;
+            if (ci < ld) {
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const int gj = j0 + (b < 4 ? tx * 4 + b : 64 + tx * 4 + b - 4);
+                    if (gj < n)
+                        DistVec<float>::store4(Dw + gj * ld + ci, acc[4 * h][b], acc[4 * h + 1][b], acc[4 * h + 2][b],
+                                               acc[4 * h + 3][b]);
+                }
+            }
+        }
+    }
+    if (__syncthreads_or(overflow) && tid == 0) atomic_status(args.status, kOverflow);
+}
+
 // ---------------------------------------------------------------------------
 // Core distances.
 // ---------------------------------------------------------------------------
 
 constexpr int kCoreRows = 128;        // rows per CTA of the points kernel
-constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel: many CTAs keep loads in flight
+constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel (one warp per row segment)
 constexpr int kCorePrefetch = 16;
+constexpr int kCoreSpanMin = 256;
+
+// Segments each row scan of the matrix kernel is split into (one warp each):
+// more loads in flight per SM; the partial lists fit 32 KB of shared memory.
+template <typename Real, int K>
+__host__ __device__ constexpr int core_segments() {
+    constexpr int s = (sizeof(Real) == 4 ? 128 : 64) / K;
+    return s < 1 ? 1 : (s > 8 ? 8 : s);
+}
 
 // Insert (d, j) into the ascending register list L/LI of length K; strict '<'
 // keeps earlier (smaller) indices ahead among equal values.
 template <typename Real, int K>
 __device__ __forceinline__ void topk_insert(Real (&L)[K], int (&LI)[K], Real d, int j) {
-    if (!(d < L[K - 1])) return;
+    using T = RealTraits<Real>;
+    if (!T::lt(d, L[K - 1])) return;
 #pragma unroll
     for (int t = K - 1; t > 0; --t) {
-        if (d < L[t - 1]) { L[t] = L[t - 1]; LI[t] = LI[t - 1]; }
-        else if (d < L[t]) { L[t] = d; LI[t] = j; }
+        const bool shift = T::lt(d, L[t - 1]);
+        const bool place = !shift && T::lt(d, L[t]);
+        L[t] = T::sel(shift, L[t - 1], T::sel(place, d, L[t]));
+        LI[t] = shift ? LI[t - 1] : (place ? j : LI[t]);
     }
-    if (d < L[0]) { L[0] = d; LI[0] = j; }
+    const bool first = T::lt(d, L[0]);
+    L[0] = T::sel(first, d, L[0]);
+    LI[0] = first ? j : LI[0];
 }
 
 template <typename Real, int K>
@@ -245,10 +407,17 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
 }
 
 // Rows from the materialized matrix: thread i reads column i (the block is
-// symmetric), so every step is one coalesced row segment.
+// symmetric), so every step is one coalesced row segment.  Warp s of the CTA
+// scans the s-th of S column ranges for the CTA's 32 rows; warp 0 then merges
+// the other warps' sorted lists in range order, which keeps (value, index)
+// order: equal values from lower ranges were inserted first.
 template <typename Real, int K>
-__global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_kernel(const CoreArgs args) {
+__global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
+    hdb_core_matrix_kernel(const CoreArgs args) {
     using T = RealTraits<Real>;
+    constexpr int S = core_segments<Real, K>();
+    __shared__ Real s_val[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
+    __shared__ int s_ix[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
     const int item = blockIdx.x;
     if (item >= args.n_items) return;
     const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
@@ -256,28 +425,52 @@ __global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_kernel(const 
     const int n = (int)(args.offsets[w + 1] - base);
     const Real* __restrict__ Dw = static_cast<const Real*>(args.dist) + args.dist_offsets[w];
     const int64_t ld = dist_ld(n);
-    const int i = r0 + threadIdx.x;
-    if (i >= n) return;
+    const int r = threadIdx.x & (kCoreMatrixRows - 1), seg = threadIdx.x / kCoreMatrixRows;
+    const int i = r0 + r;
+    const bool row = i < n;
+    // At least kCoreSpanMin columns per range: small windows use fewer warps.
+    const int ranges = max(1, min(S, n / kCoreSpanMin));
+    const int span = ((n + ranges - 1) / ranges + kCorePrefetch - 1) / kCorePrefetch * kCorePrefetch;
+    const int jlo = min(n, seg * span), jhi = min(n, jlo + span);
     Real L[K];
     int LI[K];
 #pragma unroll
     for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
-    // kCorePrefetch independent row loads in flight per thread: the pass is
-    // bound by memory latency, not by the insertions.
-    int j0 = 0;
-    for (; j0 + kCorePrefetch <= n; j0 += kCorePrefetch) {
-        Real v[kCorePrefetch];
+    if (row) {
+        // kCorePrefetch independent row loads in flight per thread.
+        int j0 = jlo;
+        for (; j0 + kCorePrefetch <= jhi; j0 += kCorePrefetch) {
+            Real v[kCorePrefetch];
 #pragma unroll
-        for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
+            for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
 #pragma unroll
-        for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
+            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
+        }
+        for (int j = j0; j < jhi; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
     }
-    for (int j = j0; j < n; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
-    Real value = Real(0);
-    int index = -1;
-    topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
-    static_cast<Real*>(args.core)[base + i] = value;
-    if (args.core_nbr) args.core_nbr[base + i] = index;
+    if constexpr (S > 1) {
+        if (seg > 0) {
+#pragma unroll
+            for (int t = 0; t < K; ++t) { s_val[seg - 1][t][r] = L[t]; s_ix[seg - 1][t][r] = LI[t]; }
+        }
+        __syncthreads();
+        if (seg == 0 && row) {
+            for (int q = 0; q < ranges - 1; ++q) {
+                for (int t = 0; t < K; ++t) {
+                    const Real d = s_val[q][t][r];
+                    if (!T::lt(d, L[K - 1])) break;  // the list is ascending
+                    topk_insert<Real, K>(L, LI, d, s_ix[q][t][r]);
+                }
+            }
+        }
+    }
+    if (seg == 0 && row) {
+        Real value = Real(0);
+        int index = -1;
+        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = value;
+        if (args.core_nbr) args.core_nbr[base + i] = index;
+    }
 }
 
 // Any ms: one CTA (256 threads) per row; the row is computed (or read) into

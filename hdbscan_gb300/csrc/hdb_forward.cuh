@@ -139,9 +139,11 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
     const int D = args.D;
 
     // Per-slot state.  Slot s = tid*SV + v; xr holds the coordinates, act marks
-    // slots holding a vertex outside the tree.  (Packed f32x2 arithmetic is not
-    // used: ptxas contracts its multiply-add chains into FMA, which changes the
-    // rounding of the distance sums.)
+    // slots holding a vertex outside the tree.  Float distances use packed
+    // f32x2 instructions for the differences and squares only; the sum stays a
+    // chain of scalar round-to-nearest adds in k order (a packed multiply
+    // feeding a packed add may be contracted into a packed FMA, which would
+    // change the rounding).
     Real xr[SV][DPS];
     Real best[SV], thr[SV], core_r[SV];
     int src[SV], vid[SV];
@@ -222,12 +224,28 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
                 Real c[VEC];
                 load_vec<Real, VEC>(c, s_x, Xw, cur, k0, DPS, xs, D);
 #pragma unroll
-                for (int v = 0; v < SV; ++v)
+                for (int v = 0; v < SV; ++v) {
+                    if constexpr (sizeof(Real) == 4) {
+                        // Two coordinates per packed instruction: x - c as
+                        // fma(c, -1, x) (exact product, one rounding: RN(x - c)
+                        // = -RN(c - x), same square), the squares as one packed
+                        // multiply, then the k-ordered scalar sum.
 #pragma unroll
-                    for (int kk = 0; kk < VEC; ++kk) {
-                        const Real delta = T::sub(c[kk], xr[v][k0 + kk]);
-                        acc[v] = T::add(acc[v], T::mul(delta, delta));
+                        for (int kk = 0; kk < VEC; kk += 2) {
+                            const float2 delta = __ffma2_rn(make_float2(c[kk], c[kk + 1]), make_float2(-1.0f, -1.0f),
+                                                            make_float2(xr[v][k0 + kk], xr[v][k0 + kk + 1]));
+                            const float2 sq = __fmul2_rn(delta, delta);
+                            acc[v] = T::add(acc[v], sq.x);
+                            acc[v] = T::add(acc[v], sq.y);
+                        }
+                    } else {
+#pragma unroll
+                        for (int kk = 0; kk < VEC; ++kk) {
+                            const Real delta = T::sub(c[kk], xr[v][k0 + kk]);
+                            acc[v] = T::add(acc[v], T::mul(delta, delta));
+                        }
                     }
+                }
             }
         } else {
             // Matrix variant: row `cur` of the window's distance block (slots

@@ -37,7 +37,8 @@ cudaError_t launch_core_points(const CoreArgs& a, int grid, cudaStream_t s, int 
 
 template <typename Real, int K>
 cudaError_t launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
-    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows, 0, s, priority, 1, a);
+    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows * core_segments<Real, K>(), 0, s,
+                     priority, 1, a);
 }
 
 template <typename Real, int K, int DP>
@@ -52,6 +53,9 @@ constexpr CoreVariant core_matrix_variant() {
 
 template <typename Real>
 cudaError_t launch_distance(const DistanceArgs& a, int grid, cudaStream_t s, int priority) {
+    if constexpr (sizeof(Real) == 4) {
+        if (a.tile == kDistTile128) return launch_ex(hdb_distance128_kernel<float>, grid, 256, 0, s, priority, 1, a);
+    }
     return launch_ex(hdb_distance_kernel<Real>, grid, 256, 0, s, priority, 1, a);
 }
 

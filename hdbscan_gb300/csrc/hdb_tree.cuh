@@ -580,7 +580,14 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
     int16_t* blocked = a.s4;
     int16_t* stop = a.s5;
     int16_t* label_map = a.s6;
-    for (int c = lane; c < clusters; c += 32) first[c] = -1;
+    int16_t* eps_side = a.s7;          // bit 0: 1/birth > epsilon, bit 1: 1/birth < epsilon
+    for (int c = lane; c < clusters; c += 32) {
+        first[c] = -1;
+        if (eps_on) {
+            const Real inv = T::recip(birth[c]);
+            eps_side[c] = (int16_t)((inv > epsilon ? 1 : 0) | (inv < epsilon ? 2 : 0));
+        }
+    }
     __syncwarp();
     for (int child = n + 1 + 2 * lane; child < next_label; child += 64) first[parent[child - n] - n] = (int16_t)child;
     __syncwarp();
@@ -593,7 +600,7 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
             for (int node = next_label - 1; node >= (allow_single ? n : n + 1); --node) {
                 const int f = first[node - n];
                 const Real subtree = f < 0 ? Real(0) : T::add(T::add(Real(0), stab[f - n]), stab[f + 1 - n]);
-                if (subtree > stab[node - n]) {
+                if (T::lt(stab[node - n], subtree)) {
                     a.sel[node - n] = 0;
                     stab[node - n] = subtree;
                 }
@@ -618,10 +625,10 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
             label_map[node - n] = -1;
             if (eps_on) {
                 const int st = anc == n ? (allow_single ? n : node)
-                                        : (T::recip(birth[anc - n]) > epsilon ? anc : stop[anc - n]);
+                                        : ((eps_side[anc - n] & 1) ? anc : stop[anc - n]);
                 stop[node - n] = (int16_t)st;
                 if (selected) {
-                    const int chosen = T::recip(birth[node - n]) < epsilon ? st : node;
+                    const int chosen = (eps_side[node - n] & 2) ? st : node;
                     label_map[chosen - n] = 1;
                 }
             }
