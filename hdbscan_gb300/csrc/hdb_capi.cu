@@ -176,7 +176,7 @@ const hdb::ForwardVariant* find_variant(const hdb::PrecisionKernels& k, int thre
 }
 
 const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int precision, int n, int D,
-                                          bool unit, bool force_matrix) {
+                                          bool unit, bool force_matrix, bool allow_cluster = true) {
     int threads, v;
     class_shape(n, &threads, &v);
     if (force_matrix) return find_variant(k, threads, v, 0);
@@ -184,7 +184,8 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
         std::lock_guard<std::mutex> lock(g_tuning_mutex);
         for (const TuningRule& r : g_tuning) {
             if ((r.precision >= 0 && r.precision != precision) || (r.unit >= 0 && r.unit != (unit ? 1 : 0)) ||
-                n > r.n_max || D > r.d_max || r.threads * r.slots * r.cluster < n || (r.dims > 0 && D > r.dims))
+                n > r.n_max || D > r.d_max || r.threads * r.slots * r.cluster < n || (r.dims > 0 && D > r.dims) ||
+                (!allow_cluster && r.cluster > 1))
                 continue;
             const hdb::ForwardVariant* f = find_variant(k, r.threads, r.slots, r.dims, r.cluster, r.per_sm);
             if (f) return f;
@@ -195,7 +196,7 @@ const hdb::ForwardVariant* choose_variant(const hdb::PrecisionKernels& k, int pr
     // CTA).  float64 SIMT is a small fraction of float32 on GB300, so float64
     // windows use the matrix variant: the distance block is computed once per
     // pair by a grid spread over every SM, and Prim only reads rows.
-    if (precision == HDB_F32 && n > 1024 && D <= 32) {
+    if (allow_cluster && precision == HDB_F32 && n > 1024 && D <= 32) {
         const int cluster = n <= 2048 ? 2 : 4;
         for (int option : {8, 16, 32})
             if (D <= option) {
@@ -267,10 +268,27 @@ int build_plan(hdb_plan* p) {
     for (int w = 0; w < p->B; ++w) order[w] = w;
     auto size_of = [&](int w) { return (int)(p->offsets[w + 1] - p->offsets[w]); };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return size_of(a) > size_of(b); });
+    std::vector<const hdb::ForwardVariant*> chosen(p->B, nullptr);
+    int ctas = 0;  // CTAs the batch occupies at once: one per window, CS per clustered window
+    for (int w : order) {
+        chosen[w] = choose_variant(k, p->precision, size_of(w), p->D, unit, force_matrix);
+        if (!chosen[w]) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(size_of(w)) + " points");
+        ctas += chosen[w]->cluster;
+    }
+    // A cluster shortens one window's Prim but holds CS SMs; once the batch
+    // needs more than one wave, the smallest clustered windows run on one CTA
+    // each, until the batch fits the SMs again.
+    for (auto it = order.rbegin(); it != order.rend() && ctas > p->sms; ++it) {
+        const int w = *it;
+        if (chosen[w]->cluster <= 1) continue;
+        const hdb::ForwardVariant* single = choose_variant(k, p->precision, size_of(w), p->D, unit, force_matrix, false);
+        if (!single) continue;
+        ctas -= chosen[w]->cluster - 1;
+        chosen[w] = single;
+    }
     for (int w : order) {
         const int n = size_of(w);
-        const hdb::ForwardVariant* fv = choose_variant(k, p->precision, n, p->D, unit, force_matrix);
-        if (!fv) return fail(HDB_E_INVALID, "no kernel variant for a window of " + std::to_string(n) + " points");
+        const hdb::ForwardVariant* fv = chosen[w];
         size_t budget = 0;
         int rc = smem_budget(fv, optin, per_sm_smem, &budget);
         if (rc) return rc;

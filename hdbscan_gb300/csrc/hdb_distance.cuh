@@ -306,34 +306,38 @@ constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel (one 
 constexpr int kCorePrefetch = 16;
 constexpr int kCoreSpanMin = 256;
 
-// Segments each row scan of the matrix kernel is split into (one warp each):
-// more loads in flight per SM; the partial lists fit 32 KB of shared memory.
+// Column ranges each row scan of the matrix kernel is split into (one warp
+// each): more loads in flight per SM, but every range fills its own list, and
+// a warp runs the insertion whenever one of its 32 rows inserts.  That pays
+// for K = 8 lists only; longer lists keep one range.
 template <typename Real, int K>
 __host__ __device__ constexpr int core_segments() {
-    constexpr int s = (sizeof(Real) == 4 ? 128 : 64) / K;
-    return s < 1 ? 1 : (s > 8 ? 8 : s);
+    return K <= 8 ? 8 : 1;
 }
 
-// Insert (d, j) into the ascending register list L/LI of length K; strict '<'
-// keeps earlier (smaller) indices ahead among equal values.
-template <typename Real, int K>
-__device__ __forceinline__ void topk_insert(Real (&L)[K], int (&LI)[K], Real d, int j) {
-    using T = RealTraits<Real>;
-    if (!T::lt(d, L[K - 1])) return;
+// The k-nearest lists hold order-preserving keys of the (non-negative)
+// distances: integer compares and moves, also for float64 (GB300 runs double
+// compares and selects on its FP64 pipe).  Insert (key, j) into the ascending
+// register list L/LI of length K; strict '<' keeps earlier (smaller) indices
+// ahead among equal values.  'below' is d < L[t], monotone in t, so position t
+// takes L[t-1] when d is below it, else d when d is below L[t].
+template <typename Key, int K>
+__device__ __forceinline__ void topk_insert(Key (&L)[K], int (&LI)[K], Key d, int j) {
+    if (!key_lt(d, L[K - 1])) return;
+    bool below = true;  // d < L[K-1]
 #pragma unroll
     for (int t = K - 1; t > 0; --t) {
-        const bool shift = T::lt(d, L[t - 1]);
-        const bool place = !shift && T::lt(d, L[t]);
-        L[t] = T::sel(shift, L[t - 1], T::sel(place, d, L[t]));
-        LI[t] = shift ? LI[t - 1] : (place ? j : LI[t]);
+        const bool below_prev = key_lt(d, L[t - 1]);
+        L[t] = key_sel(below_prev, L[t - 1], key_sel(below, d, L[t]));
+        LI[t] = below_prev ? LI[t - 1] : (below ? j : LI[t]);
+        below = below_prev;
     }
-    const bool first = T::lt(d, L[0]);
-    L[0] = T::sel(first, d, L[0]);
-    LI[0] = first ? j : LI[0];
+    L[0] = key_sel(below, d, L[0]);
+    LI[0] = below ? j : LI[0];
 }
 
-template <typename Real, int K>
-__device__ __forceinline__ void topk_pick(const Real (&L)[K], const int (&LI)[K], int k, Real& value, int& index) {
+template <typename Key, int K>
+__device__ __forceinline__ void topk_pick(const Key (&L)[K], const int (&LI)[K], int k, Key& value, int& index) {
 #pragma unroll
     for (int t = 0; t < K; ++t)
         if (t == k) { value = L[t]; index = LI[t]; }
@@ -358,10 +362,11 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
     Real xi[DP];
 #pragma unroll
     for (int k = 0; k < DP; ++k) xi[k] = (i < n && k < D) ? Xw[(int64_t)i * D + k] : Real(0);
-    Real L[K];
+    using Key = typename T::Bits;
+    Key L[K];
     int LI[K];
 #pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
+    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
     int overflow = 0;
     for (int j0 = 0; j0 < n; j0 += TJ) {
         const int cnt = min(TJ, n - j0);
@@ -391,16 +396,16 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
                 }
                 const Real d = T::sqrt_rn(acc);
                 overflow |= !(d <= T::kMax);
-                topk_insert<Real, K>(L, LI, d, j0 + jj);
+                topk_insert<Key, K>(L, LI, T::key(d), j0 + jj);
             }
         }
         __syncthreads();
     }
     if (i < n) {
-        Real value = Real(0);
+        Key value = 0;
         int index = -1;
-        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
-        static_cast<Real*>(args.core)[base + i] = value;
+        topk_pick<Key, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = T::from_key(value);
         if (args.core_nbr) args.core_nbr[base + i] = index;
     }
     if (__syncthreads_or(overflow) && threadIdx.x == 0) atomic_status(args.status, kOverflow);
@@ -416,8 +421,9 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
     hdb_core_matrix_kernel(const CoreArgs args) {
     using T = RealTraits<Real>;
     constexpr int S = core_segments<Real, K>();
-    __shared__ Real s_val[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
-    __shared__ int s_ix[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
+    using Key = typename T::Bits;
+    __shared__ Key s_val[S > 1 ? S - 1 : 1][S > 1 ? K : 1][kCoreMatrixRows];
+    __shared__ int s_ix[S > 1 ? S - 1 : 1][S > 1 ? K : 1][kCoreMatrixRows];
     const int item = blockIdx.x;
     if (item >= args.n_items) return;
     const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
@@ -432,10 +438,10 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
     const int ranges = max(1, min(S, n / kCoreSpanMin));
     const int span = ((n + ranges - 1) / ranges + kCorePrefetch - 1) / kCorePrefetch * kCorePrefetch;
     const int jlo = min(n, seg * span), jhi = min(n, jlo + span);
-    Real L[K];
+    Key L[K];
     int LI[K];
 #pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
+    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
     if (row) {
         // kCorePrefetch independent row loads in flight per thread.
         int j0 = jlo;
@@ -444,9 +450,9 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
 #pragma unroll
             for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
 #pragma unroll
-            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
+            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Key, K>(L, LI, T::key(v[u]), j0 + u);
         }
-        for (int j = j0; j < jhi; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
+        for (int j = j0; j < jhi; ++j) topk_insert<Key, K>(L, LI, T::key(__ldcs(Dw + (int64_t)j * ld + i)), j);
     }
     if constexpr (S > 1) {
         if (seg > 0) {
@@ -457,18 +463,18 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
         if (seg == 0 && row) {
             for (int q = 0; q < ranges - 1; ++q) {
                 for (int t = 0; t < K; ++t) {
-                    const Real d = s_val[q][t][r];
-                    if (!T::lt(d, L[K - 1])) break;  // the list is ascending
-                    topk_insert<Real, K>(L, LI, d, s_ix[q][t][r]);
+                    const Key d = s_val[q][t][r];
+                    if (!key_lt(d, L[K - 1])) break;  // the list is ascending
+                    topk_insert<Key, K>(L, LI, d, s_ix[q][t][r]);
                 }
             }
         }
     }
     if (seg == 0 && row) {
-        Real value = Real(0);
+        Key value = 0;
         int index = -1;
-        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
-        static_cast<Real*>(args.core)[base + i] = value;
+        topk_pick<Key, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = T::from_key(value);
         if (args.core_nbr) args.core_nbr[base + i] = index;
     }
 }

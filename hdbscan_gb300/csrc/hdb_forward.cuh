@@ -277,18 +277,22 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
                     const Real d = acc[v];
                     overflow |= !T::finite_nn(d);
                     const Real wgt = UNIT ? d : T::vmax(T::vmax(core_cur, core_r[v]), d);
-                    if (T::lt(wgt, best[v])) { best[v] = wgt; src[v] = cur; }
+                    const bool better = T::lt(wgt, best[v]);
+                    best[v] = T::sel(better, wgt, best[v]);
+                    src[v] = better ? cur : src[v];
                 }
             }
-            const Key key = act[v] ? T::key(best[v]) : SENTINEL;
+            const Key key = key_sel(act[v], T::key(best[v]), SENTINEL);
             const uint32_t j = (uint32_t)vid[v];
-            if (key_idx_lt(key, j, lkey, lidx)) { lkey = key; lidx = j; }
+            const bool better = key_idx_lt(key, j, lkey, lidx);
+            lkey = key_sel(better, key, lkey);
+            lidx = better ? j : lidx;
         }
         warp_argmin(lkey, lidx);
         const int buf = it & 1;
         if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
         bar_sync(kBarIter, aw * 32);
-        Key gk = lane < aw ? s_key[buf][lane] : SENTINEL;
+        Key gk = key_sel(lane < aw, s_key[buf][lane < aw ? lane : 0], SENTINEL);
         uint32_t gi = lane < aw ? s_idx[buf][lane] : 0xffffffffu;
         warp_argmin(gk, gi);
         const int next = (int)gi;
