@@ -97,13 +97,6 @@ __device__ __forceinline__ bool key_lt(unsigned long long a, unsigned long long 
     const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
     return ah < bh || (ah == bh && (uint32_t)a < (uint32_t)b);
 }
-// c ? a : b on 32-bit words.
-__device__ __forceinline__ uint32_t key_sel(bool c, uint32_t a, uint32_t b) { return c ? a : b; }
-__device__ __forceinline__ unsigned long long key_sel(bool c, unsigned long long a, unsigned long long b) {
-    const uint32_t hi = c ? (uint32_t)(a >> 32) : (uint32_t)(b >> 32);
-    const uint32_t lo = c ? (uint32_t)a : (uint32_t)b;
-    return ((unsigned long long)hi << 32) | lo;
-}
 template <typename Key>
 __device__ __forceinline__ bool key_idx_lt(Key k, uint32_t i, Key lk, uint32_t li) {
     return key_lt(k, lk) || (key_eq(k, lk) && i < li);

@@ -306,38 +306,37 @@ constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel (one 
 constexpr int kCorePrefetch = 16;
 constexpr int kCoreSpanMin = 256;
 
-// Column ranges each row scan of the matrix kernel is split into (one warp
-// each): more loads in flight per SM, but every range fills its own list, and
-// a warp runs the insertion whenever one of its 32 rows inserts.  That pays
-// for K = 8 lists only; longer lists keep one range.
+// Segments each row scan of the matrix kernel is split into (one warp each):
+// more loads in flight per SM; the partial lists fit 32 KB of shared memory.
+// Every segment fills its own list and a warp runs an insertion whenever one
+// of its 32 rows inserts, so float64 lists (costlier insertions) split only
+// when K = 8.
 template <typename Real, int K>
 __host__ __device__ constexpr int core_segments() {
-    return K <= 8 ? 8 : 1;
+    constexpr int s = sizeof(Real) == 4 ? 128 / K : (K <= 8 ? 8 : 1);
+    return s < 1 ? 1 : (s > 8 ? 8 : s);
 }
 
-// The k-nearest lists hold order-preserving keys of the (non-negative)
-// distances: integer compares and moves, also for float64 (GB300 runs double
-// compares and selects on its FP64 pipe).  Insert (key, j) into the ascending
-// register list L/LI of length K; strict '<' keeps earlier (smaller) indices
-// ahead among equal values.  'below' is d < L[t], monotone in t, so position t
-// takes L[t-1] when d is below it, else d when d is below L[t].
-template <typename Key, int K>
-__device__ __forceinline__ void topk_insert(Key (&L)[K], int (&LI)[K], Key d, int j) {
-    if (!key_lt(d, L[K - 1])) return;
-    bool below = true;  // d < L[K-1]
+// Insert (d, j) into the ascending register list L/LI of length K; strict '<'
+// keeps earlier (smaller) indices ahead among equal values.
+template <typename Real, int K>
+__device__ __forceinline__ void topk_insert(Real (&L)[K], int (&LI)[K], Real d, int j) {
+    using T = RealTraits<Real>;
+    if (!T::lt(d, L[K - 1])) return;
 #pragma unroll
     for (int t = K - 1; t > 0; --t) {
-        const bool below_prev = key_lt(d, L[t - 1]);
-        L[t] = key_sel(below_prev, L[t - 1], key_sel(below, d, L[t]));
-        LI[t] = below_prev ? LI[t - 1] : (below ? j : LI[t]);
-        below = below_prev;
+        const bool shift = T::lt(d, L[t - 1]);
+        const bool place = !shift && T::lt(d, L[t]);
+        L[t] = T::sel(shift, L[t - 1], T::sel(place, d, L[t]));
+        LI[t] = shift ? LI[t - 1] : (place ? j : LI[t]);
     }
-    L[0] = key_sel(below, d, L[0]);
-    LI[0] = below ? j : LI[0];
+    const bool first = T::lt(d, L[0]);
+    L[0] = T::sel(first, d, L[0]);
+    LI[0] = first ? j : LI[0];
 }
 
-template <typename Key, int K>
-__device__ __forceinline__ void topk_pick(const Key (&L)[K], const int (&LI)[K], int k, Key& value, int& index) {
+template <typename Real, int K>
+__device__ __forceinline__ void topk_pick(const Real (&L)[K], const int (&LI)[K], int k, Real& value, int& index) {
 #pragma unroll
     for (int t = 0; t < K; ++t)
         if (t == k) { value = L[t]; index = LI[t]; }
@@ -362,11 +361,10 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
     Real xi[DP];
 #pragma unroll
     for (int k = 0; k < DP; ++k) xi[k] = (i < n && k < D) ? Xw[(int64_t)i * D + k] : Real(0);
-    using Key = typename T::Bits;
-    Key L[K];
+    Real L[K];
     int LI[K];
 #pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
+    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
     int overflow = 0;
     for (int j0 = 0; j0 < n; j0 += TJ) {
         const int cnt = min(TJ, n - j0);
@@ -396,16 +394,16 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
                 }
                 const Real d = T::sqrt_rn(acc);
                 overflow |= !(d <= T::kMax);
-                topk_insert<Key, K>(L, LI, T::key(d), j0 + jj);
+                topk_insert<Real, K>(L, LI, d, j0 + jj);
             }
         }
         __syncthreads();
     }
     if (i < n) {
-        Key value = 0;
+        Real value = Real(0);
         int index = -1;
-        topk_pick<Key, K>(L, LI, args.ms - 1, value, index);
-        static_cast<Real*>(args.core)[base + i] = T::from_key(value);
+        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = value;
         if (args.core_nbr) args.core_nbr[base + i] = index;
     }
     if (__syncthreads_or(overflow) && threadIdx.x == 0) atomic_status(args.status, kOverflow);
@@ -421,9 +419,8 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
     hdb_core_matrix_kernel(const CoreArgs args) {
     using T = RealTraits<Real>;
     constexpr int S = core_segments<Real, K>();
-    using Key = typename T::Bits;
-    __shared__ Key s_val[S > 1 ? S - 1 : 1][S > 1 ? K : 1][kCoreMatrixRows];
-    __shared__ int s_ix[S > 1 ? S - 1 : 1][S > 1 ? K : 1][kCoreMatrixRows];
+    __shared__ Real s_val[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
+    __shared__ int s_ix[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
     const int item = blockIdx.x;
     if (item >= args.n_items) return;
     const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
@@ -438,10 +435,10 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
     const int ranges = max(1, min(S, n / kCoreSpanMin));
     const int span = ((n + ranges - 1) / ranges + kCorePrefetch - 1) / kCorePrefetch * kCorePrefetch;
     const int jlo = min(n, seg * span), jhi = min(n, jlo + span);
-    Key L[K];
+    Real L[K];
     int LI[K];
 #pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
+    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
     if (row) {
         // kCorePrefetch independent row loads in flight per thread.
         int j0 = jlo;
@@ -450,9 +447,9 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
 #pragma unroll
             for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
 #pragma unroll
-            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Key, K>(L, LI, T::key(v[u]), j0 + u);
+            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
         }
-        for (int j = j0; j < jhi; ++j) topk_insert<Key, K>(L, LI, T::key(__ldcs(Dw + (int64_t)j * ld + i)), j);
+        for (int j = j0; j < jhi; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
     }
     if constexpr (S > 1) {
         if (seg > 0) {
@@ -463,20 +460,82 @@ __global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
         if (seg == 0 && row) {
             for (int q = 0; q < ranges - 1; ++q) {
                 for (int t = 0; t < K; ++t) {
-                    const Key d = s_val[q][t][r];
-                    if (!key_lt(d, L[K - 1])) break;  // the list is ascending
-                    topk_insert<Key, K>(L, LI, d, s_ix[q][t][r]);
+                    const Real d = s_val[q][t][r];
+                    if (!T::lt(d, L[K - 1])) break;  // the list is ascending
+                    topk_insert<Real, K>(L, LI, d, s_ix[q][t][r]);
                 }
             }
         }
     }
     if (seg == 0 && row) {
-        Key value = 0;
+        Real value = Real(0);
         int index = -1;
-        topk_pick<Key, K>(L, LI, args.ms - 1, value, index);
-        static_cast<Real*>(args.core)[base + i] = T::from_key(value);
+        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
+        static_cast<Real*>(args.core)[base + i] = value;
         if (args.core_nbr) args.core_nbr[base + i] = index;
     }
+}
+
+// Float64 rows from the materialized matrix, as hdb_core_matrix_kernel with
+// one warp per 32 rows, but the k-nearest list holds order-preserving integer
+// keys of the (non-negative) distances and moves them as 32-bit words: GB300
+// issues double compares, double selects and 64-bit integer selects to its
+// FP64 pipe, which made the double-valued list the bound of this scan.
+__device__ __forceinline__ unsigned long long core_key_sel(bool c, unsigned long long a, unsigned long long b) {
+    const uint32_t hi = c ? (uint32_t)(a >> 32) : (uint32_t)(b >> 32);
+    const uint32_t lo = c ? (uint32_t)a : (uint32_t)b;
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// Ascending insertion of (d, j) with strict '<' (earlier indices first among
+// equal keys); 'below' = d < L[t] is monotone in t and carried down.
+template <int K>
+__device__ __forceinline__ void topk_insert_key(unsigned long long (&L)[K], int (&LI)[K], unsigned long long d, int j) {
+    if (!key_lt(d, L[K - 1])) return;
+    bool below = true;
+#pragma unroll
+    for (int t = K - 1; t > 0; --t) {
+        const bool below_prev = key_lt(d, L[t - 1]);
+        L[t] = core_key_sel(below_prev, L[t - 1], core_key_sel(below, d, L[t]));
+        LI[t] = below_prev ? LI[t - 1] : (below ? j : LI[t]);
+        below = below_prev;
+    }
+    L[0] = core_key_sel(below, d, L[0]);
+    LI[0] = below ? j : LI[0];
+}
+
+template <int K>
+__global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_key_kernel(const CoreArgs args) {
+    using T = RealTraits<double>;
+    const int item = blockIdx.x;
+    if (item >= args.n_items) return;
+    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const double* __restrict__ Dw = static_cast<const double*>(args.dist) + args.dist_offsets[w];
+    const int64_t ld = dist_ld(n);
+    const int i = r0 + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long L[K];
+    int LI[K];
+#pragma unroll
+    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
+    int j0 = 0;
+    for (; j0 + kCorePrefetch <= n; j0 += kCorePrefetch) {
+        double v[kCorePrefetch];
+#pragma unroll
+        for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
+#pragma unroll
+        for (int u = 0; u < kCorePrefetch; ++u) topk_insert_key<K>(L, LI, T::key(v[u]), j0 + u);
+    }
+    for (int j = j0; j < n; ++j) topk_insert_key<K>(L, LI, T::key(__ldcs(Dw + (int64_t)j * ld + i)), j);
+    unsigned long long value = 0;
+    int index = -1;
+#pragma unroll
+    for (int t = 0; t < K; ++t)
+        if (t == args.ms - 1) { value = L[t]; index = LI[t]; }
+    static_cast<double*>(args.core)[base + i] = T::from_key(value);
+    if (args.core_nbr) args.core_nbr[base + i] = index;
 }
 
 // Any ms: one CTA (256 threads) per row; the row is computed (or read) into

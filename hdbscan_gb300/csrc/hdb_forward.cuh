@@ -277,22 +277,18 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
                     const Real d = acc[v];
                     overflow |= !T::finite_nn(d);
                     const Real wgt = UNIT ? d : T::vmax(T::vmax(core_cur, core_r[v]), d);
-                    const bool better = T::lt(wgt, best[v]);
-                    best[v] = T::sel(better, wgt, best[v]);
-                    src[v] = better ? cur : src[v];
+                    if (T::lt(wgt, best[v])) { best[v] = wgt; src[v] = cur; }
                 }
             }
-            const Key key = key_sel(act[v], T::key(best[v]), SENTINEL);
+            const Key key = act[v] ? T::key(best[v]) : SENTINEL;
             const uint32_t j = (uint32_t)vid[v];
-            const bool better = key_idx_lt(key, j, lkey, lidx);
-            lkey = key_sel(better, key, lkey);
-            lidx = better ? j : lidx;
+            if (key_idx_lt(key, j, lkey, lidx)) { lkey = key; lidx = j; }
         }
         warp_argmin(lkey, lidx);
         const int buf = it & 1;
         if (lane == 0) { s_key[buf][warp] = lkey; s_idx[buf][warp] = lidx; }
         bar_sync(kBarIter, aw * 32);
-        Key gk = key_sel(lane < aw, s_key[buf][lane < aw ? lane : 0], SENTINEL);
+        Key gk = lane < aw ? s_key[buf][lane] : SENTINEL;
         uint32_t gi = lane < aw ? s_idx[buf][lane] : 0xffffffffu;
         warp_argmin(gk, gi);
         const int next = (int)gi;
