@@ -203,3 +203,29 @@ def test_cluster_graph_replay_is_stable(cuda, precision):
         torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert torch.equal(first, labels)
+
+
+def test_cluster_rule_holds_one_wave(cuda):
+    """A cluster rule applies while the batch fits one wave of SMs; beyond it
+    the smallest clustered windows run on one CTA each (largest keep CS SMs)."""
+    import torch
+
+    from hdbscan_gb300._cuda import Plan
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rng = np.random.default_rng(11)
+    with forced_variant("float32", 512, 2, 8, 4):
+        few = np.concatenate([[0], np.cumsum(rng.integers(1100, 4000, max(sms // 8, 1)))]).astype(np.int64)
+        classes = json.loads(Plan(few, 8, min_cluster_size=5, min_samples=4).describe())["classes"]
+        assert all(c["cluster"] == 4 for c in classes), classes
+        sizes = np.sort(rng.integers(1100, 4000, sms // 2 + 10))[::-1]
+        many = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        classes = json.loads(Plan(many, 8, min_cluster_size=5, min_samples=4).describe())["classes"]
+        clustered = [c for c in classes if c["cluster"] > 1]
+        single = [c for c in classes if c["cluster"] == 1]
+        assert clustered and single, classes
+        assert sum(c["cluster"] * c["windows"] for c in classes) <= sms, classes
+        assert sum(c["windows"] for c in classes) == len(sizes)
+        n_clustered = sum(c["windows"] for c in clustered)
+        assert min(c["nmax"] for c in clustered) >= sizes[n_clustered - 1]  # the largest windows keep the cluster
+        assert max(c["nmax"] for c in single) <= sizes[n_clustered]

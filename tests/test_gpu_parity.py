@@ -119,3 +119,12 @@ def test_max_window_4096(cuda, precision):
     centers = rng.normal(0, 3, (6, 8))
     x = centers[np.arange(4096) % 6] + rng.normal(0, 0.3, (4096, 8))
     _compare([x], 16, 8, 0.0, precision)
+
+
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+@pytest.mark.parametrize("ms", [20, 40])
+def test_long_core_lists_match_oracle(cuda, precision, ms):
+    # 32- and 64-entry k-nearest lists over materialized blocks: float32 scans
+    # split into column ranges, float64 scans on integer keys; duplicated
+    # points give tied core distances.
+    _compare(_windows(ms, 6, (ms + 10, 900), 6), 8, ms, 0.0, precision, force_matrix=True)
