@@ -8,12 +8,17 @@
 //   per pair the coordinates are accumulated in k order with
 //   total = total + delta*delta and no FMA, then a correctly rounded sqrt.
 //   Block row stride ld = round_up(n, 4) keeps every row 16-byte aligned.
+// * hdb_distance128_kernel: the same blocks for float32 windows of 384 points
+//   and more, 128x128 tiles with 8x8 pairs per thread (same arithmetic).
 // * hdb_core_points_kernel / hdb_core_matrix_kernel: core_i = the (ms-1)-th
 //   smallest distance of row i, self (0) included (reference:
 //   hdbscan_gpu/_cuda.py:114-118, cp.partition).  One thread per row keeps a
 //   sorted register list of the KMAX smallest (value, index) pairs; the value
 //   at position ms-1 is the order statistic, the index is the ms-th nearest
-//   neighbour in (distance, index) order (used by the backward pass).
+//   neighbour in (distance, index) order (used by the backward pass).  The
+//   matrix kernel splits each row scan over column ranges (one warp each);
+//   hdb_core_matrix_key_kernel serves float64 lists longer than 8 with
+//   integer order keys.
 // * hdb_core_select_kernel: any ms, one CTA per row, radix select on the
 //   order-preserving bit pattern of the non-negative distances.
 #pragma once
