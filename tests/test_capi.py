@@ -69,3 +69,24 @@ def test_noalloc_rejects_oversized_batches_before_touching_the_device(lib):
     rc = lib.hdb_cluster_noalloc(0, ctypes.c_void_p(16), 65, 4096, 8, 5, 5, 0.0, ctypes.c_void_p(16), None, None)
     assert rc == -1
     assert "no-allocation limit" in lib.hdb_last_error().decode()
+
+
+def test_committed_tuning_table_names_compiled_variants(lib):
+    """Every rule of the committed autotune table names a compiled forward
+    variant that can hold its bucket, and the library accepts the table."""
+    import json
+
+    from hdbscan_gb300 import _lib, autotune
+
+    table = json.loads(autotune.TABLE.read_text())
+    assert table["fields"] == ["precision", "unit_core", "n_max", "d_max", "threads", "slots", "dims", "cluster",
+                               "per_sm"]
+    compiled = {code: set(autotune.variants(lib, code)) for code in (_lib.HDB_F32, _lib.HDB_F64)}
+    assert table["rules"]
+    for entry in table["rules"]:
+        precision, unit, n_max, d_max, threads, slots, dims, cluster, per_sm = entry["rule"]
+        assert (threads, slots, dims, cluster, per_sm) in compiled[precision], entry["rule"]
+        assert threads * slots * cluster >= n_max, entry["rule"]
+        assert dims == 0 or d_max <= dims, entry["rule"]
+        assert unit in (0, 1)
+    assert autotune.apply_table(lib) == len(table["rules"])
