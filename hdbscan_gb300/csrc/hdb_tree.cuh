@@ -591,60 +591,118 @@ __device__ void select_and_label_warp(const Arena<Real>& a, int n, int next_labe
     __syncwarp();
     for (int child = n + 1 + 2 * lane; child < next_label; child += 64) first[parent[child - n] - n] = (int16_t)child;
     __syncwarp();
-    int single_root = 0;
-    if (lane == 0) {
-        // 1. Candidates: excess of mass, children (larger ids) before parents;
-        //    or the leaves of the cluster tree (none if the root never splits).
-        if (method == 0) {
-            a.sel[0] = allow_single ? 1 : 0;
-            for (int node = next_label - 1; node >= (allow_single ? n : n + 1); --node) {
-                const int f = first[node - n];
-                const Real subtree = f < 0 ? Real(0) : T::add(T::add(Real(0), stab[f - n]), stab[f + 1 - n]);
-                if (T::lt(stab[node - n], subtree)) {
-                    a.sel[node - n] = 0;
-                    stab[node - n] = subtree;
+    // The three passes below restate the reference's serial loops over the
+    // clusters in chunks of 32 consecutive ids, one lane per cluster.  A
+    // cluster depends only on final values of its children (pass 1) or its
+    // parent (passes 2, 3); parent ids are smaller than child ids, so a lane
+    // computes once every dependency lies in an earlier chunk or belongs to a
+    // lane of this chunk that is done (a ballot per round), and the results
+    // equal the serial order's.
+    constexpr unsigned kFull = 0xffffffffu;
+    // 1. Candidates: excess of mass, children (larger ids) before parents;
+    //    or the leaves of the cluster tree (none if the root never splits).
+    if (method == 0) {
+        if (lane == 0) a.sel[0] = allow_single ? 1 : 0;
+        const int lo_node = allow_single ? n : n + 1;
+        for (int hi = next_label - 1; hi >= lo_node; hi -= 32) {
+            const int node = hi - lane;
+            bool done = node < lo_node;
+            const int f = done ? -1 : first[node - n];
+            unsigned done_mask = __ballot_sync(kFull, done);
+            // Each round finishes at least one lane of a valid tree: at most 32 rounds.
+        for (int round = 0; done_mask != kFull && round < 32; ++round) {
+                if (!done) {
+                    const bool c0 = f < 0 || f > hi || ((done_mask >> (hi - f)) & 1u);
+                    const bool c1 = f < 0 || f + 1 > hi || ((done_mask >> (hi - f - 1)) & 1u);
+                    if (c0 && c1) {
+                        const Real subtree = f < 0 ? Real(0) : T::add(T::add(Real(0), stab[f - n]), stab[f + 1 - n]);
+                        if (T::lt(stab[node - n], subtree)) {
+                            a.sel[node - n] = 0;
+                            stab[node - n] = subtree;
+                        }
+                        done = true;
+                    }
                 }
+                __syncwarp();
+                done_mask = __ballot_sync(kFull, done);
             }
-        } else {
-            a.sel[0] = 0;
-            for (int node = n + 1; node < next_label; ++node) a.sel[node - n] = first[node - n] < 0 ? 1 : 0;
         }
-        // 2. Parents first (ascending ids): suppress the descendants of a
-        //    selected cluster; with epsilon, mark the cluster each surviving
-        //    selection resolves to (itself, or its epsilon stop ancestor; the
-        //    climb ends below the root, at the root with allow_single).
+    } else {
+        if (lane == 0) a.sel[0] = 0;
+        for (int node = n + 1 + lane; node < next_label; node += 32) a.sel[node - n] = first[node - n] < 0 ? 1 : 0;
+    }
+    __syncwarp();
+    // 2. Parents first (ascending ids): suppress the descendants of a selected
+    //    cluster; with epsilon, find each cluster's epsilon stop ancestor (the
+    //    climb ends below the root, at the root with allow_single), then mark
+    //    the cluster every surviving selection resolves to (itself or its stop).
+    if (lane == 0) {
         blocked[0] = a.sel[0];
         label_map[0] = (eps_on && a.sel[0]) ? 1 : -1;  // 1/birth(root) = inf: the root never climbs
-        for (int node = n + 1; node < next_label; ++node) {
-            const int anc = parent[node - n];
-            const int inherited = blocked[anc - n];
-            int selected = a.sel[node - n];
-            blocked[node - n] = (int16_t)(inherited || selected);
-            if (inherited) selected = 0;
-            a.sel[node - n] = (uint8_t)selected;
-            label_map[node - n] = -1;
-            if (eps_on) {
-                const int st = anc == n ? (allow_single ? n : node)
-                                        : ((eps_side[anc - n] & 1) ? anc : stop[anc - n]);
-                stop[node - n] = (int16_t)st;
-                if (selected) {
-                    const int chosen = (eps_side[node - n] & 2) ? st : node;
-                    label_map[chosen - n] = 1;
-                }
-            }
-        }
-        // 3. Ascending: final selection, label numbers (the root first when
-        //    selected), nearest selected cluster of every cluster.
-        int label = 0;
-        for (int node = n; node < next_label; ++node) {
-            const int selected = eps_on ? (label_map[node - n] == 1) : a.sel[node - n];
-            a.sel[node - n] = (uint8_t)selected;
-            label_map[node - n] = (int16_t)(selected ? label++ : -1);
-            resolved[node - n] = (int16_t)(selected ? node : (node == n ? -1 : resolved[parent[node - n] - n]));
-        }
-        single_root = allow_single && label == 1 && a.sel[0];
     }
-    single_root = __shfl_sync(0xffffffffu, single_root, 0);
+    __syncwarp();
+    for (int lo = n + 1; lo < next_label; lo += 32) {
+        const int node = lo + lane;
+        bool done = node >= next_label;
+        const int anc = done ? n : parent[node - n];
+        if (!done) label_map[node - n] = -1;
+        unsigned done_mask = __ballot_sync(kFull, done);
+        // Each round finishes at least one lane of a valid tree: at most 32 rounds.
+        for (int round = 0; done_mask != kFull && round < 32; ++round) {
+            if (!done && (anc < lo || ((done_mask >> (anc - lo)) & 1u))) {
+                const int inherited = blocked[anc - n];
+                int selected = a.sel[node - n];
+                blocked[node - n] = (int16_t)(inherited || selected);
+                if (inherited) selected = 0;
+                a.sel[node - n] = (uint8_t)selected;
+                if (eps_on)
+                    stop[node - n] = (int16_t)(anc == n ? (allow_single ? n : node)
+                                                        : ((eps_side[anc - n] & 1) ? anc : stop[anc - n]));
+                done = true;
+            }
+            __syncwarp();
+            done_mask = __ballot_sync(kFull, done);
+        }
+    }
+    __syncwarp();
+    if (eps_on) {
+        for (int node = n + 1 + lane; node < next_label; node += 32)
+            if (a.sel[node - n]) label_map[((eps_side[node - n] & 2) ? stop[node - n] : node) - n] = 1;
+        __syncwarp();
+    }
+    // 3. Ascending: final selection, label numbers (a ballot prefix; the root
+    //    first when selected), nearest selected cluster of every cluster.
+    int label = 0;  // warp-uniform
+    for (int lo = n; lo < next_label; lo += 32) {
+        const int node = lo + lane;
+        const bool valid = node < next_label;
+        int selected = 0;
+        if (valid) selected = eps_on ? (label_map[node - n] == 1) : a.sel[node - n];
+        const unsigned sel_mask = __ballot_sync(kFull, valid && selected);
+        if (valid) {
+            a.sel[node - n] = (uint8_t)selected;
+            label_map[node - n] = (int16_t)(selected ? label + __popc(sel_mask & lanemask_lt()) : -1);
+        }
+        label += __popc(sel_mask);
+        bool done = !valid;
+        const int par = (valid && node != n) ? parent[node - n] : n;
+        if (valid && (selected || node == n)) {
+            resolved[node - n] = (int16_t)(selected ? node : -1);
+            done = true;
+        }
+        __syncwarp();
+        unsigned done_mask = __ballot_sync(kFull, done);
+        // Each round finishes at least one lane of a valid tree: at most 32 rounds.
+        for (int round = 0; done_mask != kFull && round < 32; ++round) {
+            if (!done && (par < lo || ((done_mask >> (par - lo)) & 1u))) {
+                resolved[node - n] = resolved[par - n];
+                done = true;
+            }
+            __syncwarp();
+            done_mask = __ballot_sync(kFull, done);
+        }
+    }
+    const int single_root = allow_single && label == 1 && a.sel[0];
     __syncwarp();
     // Points: the nearest selected cluster's label; below a lone selected root
     // (allow_single) a point joins at lambda >= 1/eps, or >= the largest
