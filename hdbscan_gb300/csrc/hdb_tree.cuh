@@ -35,7 +35,9 @@
 //    afterwards from their lowest large ancestor.
 //  * selection uses the binary shape of the condensed tree (every split
 //    creates exactly two consecutive ids), as the reference's
-//    COOPERATIVE_BINARY_EOM variant does (_kernels.py:648-669).
+//    COOPERATIVE_BINARY_EOM variant does (_kernels.py:648-669), and runs its
+//    serial passes in chunks of 32 cluster ids, one lane per cluster, each
+//    lane waiting (by ballot) only for its parent or children.
 #pragma once
 #include "hdb_common.cuh"
 
