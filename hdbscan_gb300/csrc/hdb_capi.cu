@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <list>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -98,7 +99,15 @@ struct hdb_plan {
     unsigned char* h_tables = nullptr;      // pinned
     std::vector<cudaStream_t> aux;          // one per class (empty: everything on the caller's stream)
     std::vector<cudaEvent_t> events;        // [2i] class i inputs ready, [2i+1] class i done
+    cudaEvent_t uploaded = nullptr;         // after the latest (uncaptured) upload of h_tables
     cudaGraphExec_t graph = nullptr;
+    // Serializes the host-side enqueue of forward, capture and backward calls:
+    // the fork/join events and class streams above are shared by every call,
+    // and cudaStreamWaitEvent waits on an event's latest record at the time of
+    // the call, so each call's record/wait pairs must not interleave with
+    // another thread's.  Work of concurrent calls then orders on the class
+    // streams; each call still joins only its own forwards.
+    std::mutex enqueue;
 };
 
 namespace hdb {
@@ -460,6 +469,8 @@ int build_plan(hdb_plan* p) {
     if (p->prepared) ws += (size_t)p->T * (size_t)p->D * rb;
     p->ws_bytes = align_up(std::max<size_t>(ws, 256), 256);
 
+    HDB_CUDA(cudaEventCreateWithFlags(&p->uploaded, cudaEventDisableTiming));
+
     // ---- streams for concurrent classes ------------------------------------
     const bool fork = !(p->flags & HDB_FLAG_NO_GRAPH_STREAMS) && p->classes.size() > 1;
     if (fork) {
@@ -500,8 +511,41 @@ int check_workspace(const hdb_plan* p, void* ws, size_t bytes) {
     return HDB_OK;
 }
 
+// Records p->uploaded after an upload from the pinned table image, so that
+// destroying the plan can wait for copies still reading it.  Skipped while the
+// stream is being captured (the graph's copy runs at replay time, and the
+// graph belongs to the plan).
+cudaError_t note_upload(hdb_plan* p, cudaStream_t stream) {
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &capturing);
+    if (e != cudaSuccess || capturing != cudaStreamCaptureStatusNone) return e;
+    return cudaEventRecord(p->uploaded, stream);
+}
+
+// Optional per-launch timing of run_forward (hdb_plan_profile): each kernel
+// launch is bracketed by two events on the caller's stream and tagged with its
+// phase (HDB_PHASE_*).
+struct Spans {
+    std::vector<int> phase;
+    std::vector<cudaEvent_t> events;  // start, stop per launch
+    cudaError_t begin(int ph, cudaStream_t s) {
+        cudaEvent_t e[2];
+        for (auto& x : e) {
+            cudaError_t r = cudaEventCreate(&x);
+            if (r != cudaSuccess) return r;
+            events.push_back(x);
+        }
+        phase.push_back(ph);
+        return cudaEventRecord(e[0], s);
+    }
+    cudaError_t end(cudaStream_t s) { return cudaEventRecord(events.back(), s); }
+    ~Spans() {
+        for (auto e : events) cudaEventDestroy(e);
+    }
+};
+
 int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t* status,
-                const hdb_exports_t* ex, cudaStream_t stream) {
+                const hdb_exports_t* ex, cudaStream_t stream, Spans* spans = nullptr) {
     const hdb::PrecisionKernels& k = *p->k;
     unsigned char* ws = static_cast<unsigned char*>(ws_v);
     const bool unit = p->ms <= 2;
@@ -509,10 +553,13 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
     std::memset(&none, 0, sizeof(none));
     if (!ex) ex = &none;
     HDB_CUDA(cudaMemcpyAsync(ws, p->h_tables, p->tables_bytes, cudaMemcpyHostToDevice, stream));
+    HDB_CUDA(note_upload(p, stream));
     if (status) HDB_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), stream));
     if (p->prepared) {  // producer stage: every later kernel reads the converted / normalised copy
+        if (spans) HDB_CUDA(spans->begin(HDB_PHASE_PREPARE, stream));
         HDB_CUDA(k.launch_prepare(X, p->input_type, ws + p->w_prep, p->T, p->D, p->normalize, stream,
                                   p->classes.empty() ? 0 : p->classes[0].priority));
+        if (spans) HDB_CUDA(spans->end(stream));
         X = ws + p->w_prep;
     }
     const int64_t* d_offsets = reinterpret_cast<const int64_t*>(ws + p->t_offsets);
@@ -526,7 +573,7 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
     if (ex->cl_parent && (!ex->cl_birth || !ex->cl_stability || !ex->cl_selected || !ex->point_parent || !ex->n_clusters))
         return fail(HDB_E_INVALID, "cl_parent needs cl_birth, cl_stability, cl_selected, point_parent, n_clusters");
 
-    const bool fork = !p->aux.empty();
+    const bool fork = !p->aux.empty() && !spans;
     for (size_t i = 0; i < p->classes.size(); ++i) {
         const WindowClass& c = p->classes[i];
         // 1. distance blocks of this class's matrix-variant windows (caller's stream)
@@ -541,7 +588,9 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
             a.dist = dist;
             a.dist_offsets = d_dist_off;
             a.status = status;
+            if (spans) HDB_CUDA(spans->begin(HDB_PHASE_DISTANCE, stream));
             HDB_CUDA(k.launch_distance(a, a.n_tiles, stream, c.priority));
+            if (spans) HDB_CUDA(spans->end(stream));
         }
         // 2. core distances of its windows (caller's stream)
         for (const auto& cl : c.cores) {
@@ -557,8 +606,10 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
             a.core = core;
             a.core_nbr = core_nbr;
             a.status = status;
+            if (spans) HDB_CUDA(spans->begin(HDB_PHASE_CORE, stream));
             if (cl.cv) HDB_CUDA(cl.cv->launch(a, a.n_items, stream, c.priority));
             else HDB_CUDA(k.launch_select(a, a.n_items, cl.select_smem, stream, c.priority));
+            if (spans) HDB_CUDA(spans->end(stream));
         }
         cudaStream_t s = stream;
         if (fork) {
@@ -601,9 +652,17 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
         a.point_parent = ex->point_parent;
         a.stage_ns = ex->stage_ns;
         a.probabilities = ex->probabilities;
+        a.cl_size = ex->cl_size;
+        a.point_lambda = ex->point_lambda;
+        if (p->flags & HDB_FLAG_TEST_STALL) {
+            a.stall_first_ticket = 1;
+            a.wait_limit_ns = 1000000;  // 1 ms
+        }
         a.method = (p->flags & HDB_FLAG_LEAF) ? 1 : 0;
         a.allow_single = (p->flags & HDB_FLAG_ALLOW_SINGLE) ? 1 : 0;
+        if (spans) HDB_CUDA(spans->begin(HDB_PHASE_FORWARD, s));
         HDB_CUDA(c.fv->launch(a, c.grid, c.smem, s, c.priority));
+        if (spans) HDB_CUDA(spans->end(s));
         if (fork) HDB_CUDA(cudaEventRecord(p->events[2 * i + 1], s));
     }
     if (fork)
@@ -612,6 +671,9 @@ int run_forward(hdb_plan* p, const void* X, int32_t* labels, void* ws_v, int32_t
 }
 
 // ---- plan cache of the dense seam -----------------------------------------
+// Plans are shared: a call holds its own reference while it enqueues, so
+// evicting the least recently used entry only drops the cache's reference and
+// never frees a plan another thread is still using.
 struct CacheKey {
     int precision, batch, n, dims, mcs, ms, device;
     uint64_t eps_bits;
@@ -620,43 +682,59 @@ struct CacheKey {
                ms == o.ms && device == o.device && eps_bits == o.eps_bits;
     }
 };
+using PlanRef = std::shared_ptr<hdb_plan>;
+constexpr size_t kCachedPlans = 16;
 std::mutex g_cache_mutex;
-std::list<std::pair<CacheKey, hdb_plan*>> g_cache;
+std::list<std::pair<CacheKey, PlanRef>> g_cache;
 
-int cached_plan(int precision, int batch, int n, int dims, int mcs, int ms, double eps, hdb_plan** out) {
+int cached_plan(int precision, int batch, int n, int dims, int mcs, int ms, double eps, PlanRef* out) {
     int device = 0;
     HDB_CUDA(cudaGetDevice(&device));
     CacheKey key{precision, batch, n, dims, mcs, ms, device, 0};
     std::memcpy(&key.eps_bits, &eps, sizeof(eps));
-    std::lock_guard<std::mutex> lock(g_cache_mutex);
-    for (auto it = g_cache.begin(); it != g_cache.end(); ++it) {
-        if (it->first == key) {
-            g_cache.splice(g_cache.begin(), g_cache, it);
-            *out = it->second;
-            return HDB_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mutex);
+        for (auto it = g_cache.begin(); it != g_cache.end(); ++it) {
+            if (it->first == key) {
+                g_cache.splice(g_cache.begin(), g_cache, it);
+                *out = it->second;
+                return HDB_OK;
+            }
         }
     }
     if ((int64_t)batch * n > INT32_MAX) return fail(HDB_E_INVALID, "batch * n exceeds int32");
     std::vector<int64_t> offsets((size_t)batch + 1);
     for (int b = 0; b <= batch; ++b) offsets[b] = (int64_t)b * n;
-    hdb_plan* p = nullptr;
-    int rc = hdb_plan_create(&p, precision, batch, offsets.data(), dims, mcs, ms, eps, 0);
+    hdb_plan* raw = nullptr;
+    int rc = hdb_plan_create(&raw, precision, batch, offsets.data(), dims, mcs, ms, eps, 0);
     if (rc) return rc;
-    g_cache.emplace_front(key, p);
-    if (g_cache.size() > 16) {
-        hdb_plan_destroy(g_cache.back().second);
-        g_cache.pop_back();
+    PlanRef plan(raw, hdb_plan_destroy);
+    PlanRef evicted;  // released after the cache lock
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mutex);
+        for (auto it = g_cache.begin(); it != g_cache.end(); ++it) {
+            if (it->first == key) {  // another thread built the same plan meanwhile
+                g_cache.splice(g_cache.begin(), g_cache, it);
+                *out = it->second;
+                return HDB_OK;  // `plan` is destroyed on return
+            }
+        }
+        g_cache.emplace_front(key, plan);
+        if (g_cache.size() > kCachedPlans) {
+            evicted = std::move(g_cache.back().second);
+            g_cache.pop_back();
+        }
     }
-    *out = p;
+    *out = std::move(plan);
     return HDB_OK;
 }
 
 int cluster_dense(int precision, const void* X, int batch, int n, int dims, int mcs, int ms, double eps,
                   int32_t* labels, void* ws, size_t ws_bytes, int32_t* status, void* stream) {
-    hdb_plan* p = nullptr;
+    PlanRef p;
     int rc = cached_plan(precision, batch, n, dims, mcs, ms, eps, &p);
     if (rc) return rc;
-    return hdb_plan_forward(p, X, labels, ws, ws_bytes, status, nullptr, stream);
+    return hdb_plan_forward(p.get(), X, labels, ws, ws_bytes, status, nullptr, stream);
 }
 
 }  // namespace
@@ -768,6 +846,11 @@ int hdb_plan_create(hdb_plan_t** out, int precision, int windows, const int64_t*
 
 int hdb_plan_destroy(hdb_plan_t* p) {
     if (!p) return HDB_OK;
+    // A copy from the pinned table image may still be queued on some stream.
+    if (p->uploaded) {
+        cudaEventSynchronize(p->uploaded);
+        cudaEventDestroy(p->uploaded);
+    }
     if (p->graph) cudaGraphExecDestroy(p->graph);
     for (auto s : p->aux) cudaStreamDestroy(s);
     for (auto e : p->events) cudaEventDestroy(e);
@@ -777,6 +860,16 @@ int hdb_plan_destroy(hdb_plan_t* p) {
 }
 
 size_t hdb_plan_workspace_bytes(const hdb_plan_t* p) { return p ? p->ws_bytes : 0; }
+
+// Sum over a class's windows of n (power 1) or n^2 (power 2).
+static int64_t class_points(const hdb_plan* p, const WindowClass& c, int power) {
+    int64_t total = 0;
+    for (int w : c.windows) {
+        const int64_t n = p->offsets[w + 1] - p->offsets[w];
+        total += power == 2 ? n * n : n;
+    }
+    return total;
+}
 
 int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
     if (!p || !buffer || !size) return fail(HDB_E_INVALID, "describe needs a plan and a buffer");
@@ -794,8 +887,9 @@ int hdb_plan_describe(const hdb_plan_t* p, char* buffer, size_t size) {
              "\",\"x_in_smem\":" + std::to_string(c.x_in_smem) + ",\"arenas\":" + std::to_string(c.n_arenas) +
              ",\"distance_tiles\":" + std::to_string(c.n_tiles) + ",\"tile\":" + std::to_string(c.tile) +
              ",\"priority\":" + std::to_string(c.priority) +
-             ",\"windows\":" +
-             std::to_string(c.windows.size()) + ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
+             ",\"windows\":" + std::to_string(c.windows.size()) + ",\"points\":" +
+             std::to_string(class_points(p, c, 1)) + ",\"sum_n2\":" + std::to_string(class_points(p, c, 2)) +
+             ",\"nmax\":" + std::to_string(c.nmax) + ",\"smem\":" +
              std::to_string(c.smem) + ",\"grid\":" + std::to_string(c.grid) + "}";
     }
     s += "],\"core\":[";
@@ -821,7 +915,36 @@ int hdb_plan_forward(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, si
     if (rc) return rc;
     rc = check_workspace(p, ws, ws_bytes);
     if (rc) return rc;
+    std::lock_guard<std::mutex> lock(p->enqueue);
     return run_forward(p, X, labels, ws, status, exports, static_cast<cudaStream_t>(stream));
+}
+
+int hdb_plan_profile(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, size_t ws_bytes, int32_t* status,
+                     const hdb_exports_t* exports, void* stream_v, double* phase_ms, int32_t* phase_launches) {
+    if (!p || !X || !labels || !phase_ms) return fail(HDB_E_INVALID, "plan, X, labels and phase_ms are required");
+    int rc = check_device(p);
+    if (rc) return rc;
+    rc = check_workspace(p, ws, ws_bytes);
+    if (rc) return rc;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+    Spans spans;
+    {
+        std::lock_guard<std::mutex> lock(p->enqueue);
+        rc = run_forward(p, X, labels, ws, status, exports, stream, &spans);
+    }
+    if (rc) return rc;
+    HDB_CUDA(cudaStreamSynchronize(stream));
+    for (int i = 0; i < HDB_PHASES; ++i) {
+        phase_ms[i] = 0;
+        if (phase_launches) phase_launches[i] = 0;
+    }
+    for (size_t i = 0; i < spans.phase.size(); ++i) {
+        float ms = 0;
+        HDB_CUDA(cudaEventElapsedTime(&ms, spans.events[2 * i], spans.events[2 * i + 1]));
+        phase_ms[spans.phase[i]] += ms;
+        if (phase_launches) ++phase_launches[spans.phase[i]];
+    }
+    return HDB_OK;
 }
 
 int hdb_plan_capture(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, size_t ws_bytes, int32_t* status,
@@ -834,6 +957,9 @@ int hdb_plan_capture(hdb_plan_t* p, const void* X, int32_t* labels, void* ws, si
     cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
     cudaStream_t capture = stream;
     bool own = false;
+    // The class streams join the capture until it ends: no other call may
+    // enqueue on them meanwhile.
+    std::lock_guard<std::mutex> lock(p->enqueue);
     if (!capture) {  // the legacy stream cannot be captured
         HDB_CUDA(cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking));
         own = true;
@@ -861,6 +987,7 @@ int hdb_plan_replay(hdb_plan_t* p, void* stream) {
     if (!p || !p->graph) return fail(HDB_E_INVALID, "plan has no captured graph");
     int rc = check_device(p);
     if (rc) return rc;
+    std::lock_guard<std::mutex> lock(p->enqueue);
     HDB_CUDA(cudaGraphLaunch(p->graph, static_cast<cudaStream_t>(stream)));
     return HDB_OK;
 }
@@ -881,7 +1008,9 @@ int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, con
     if (rc) return rc;
     unsigned char* ws = static_cast<unsigned char*>(ws_v);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lock(p->enqueue);
     HDB_CUDA(cudaMemcpyAsync(ws, p->h_tables, p->tables_bytes, cudaMemcpyHostToDevice, s));
+    HDB_CUDA(note_upload(p, s));
     hdb::BackwardArgs a{};
     a.X = X;
     a.offsets = reinterpret_cast<const int64_t*>(ws + p->t_offsets);
@@ -901,7 +1030,7 @@ int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, con
 }
 
 size_t hdb_cluster_workspace_bytes(int precision, int batch, int n, int dims, int mcs, int ms) {
-    hdb_plan* p = nullptr;
+    PlanRef p;
     if (cached_plan(precision, batch, n, dims, mcs, ms, 0.0, &p)) return 0;
     return p->ws_bytes;
 }

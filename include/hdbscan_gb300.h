@@ -23,6 +23,19 @@
  *  - The device status word is a bit-or of HDB_STATUS_*; it is zeroed by each
  *    forward call and read by the caller after synchronizing (the reference
  *    raises at its two host syncs, _cuda.py:98-99 and :112-113).
+ *  - Threading: every entry point may be called from any host thread and any
+ *    stream.  Calls on one plan (forward, capture, replay, backward) enqueue
+ *    one at a time under the plan's lock; each call waits only for its own
+ *    work.  The dense entry points share plans from a cache of 16 shapes and
+ *    hold a reference while they enqueue, so eviction never frees a plan in
+ *    use.  Concurrent calls must not share a workspace, labels or status.
+ *    While a caller's own stream capture holds a plan's forward (not
+ *    hdb_plan_capture), other threads must not use that plan until the
+ *    capture ends.
+ *  - Window sizes (offsets) are host data given at plan creation: the plan
+ *    chooses kernels and sorts windows into its work queues from them.  A
+ *    caller whose offsets live on the device copies them to the host once
+ *    per batch shape, then reuses the plan (or its captured graph).
  */
 #ifndef HDBSCAN_GB300_H
 #define HDBSCAN_GB300_H
@@ -71,6 +84,12 @@ extern "C" {
 #define HDB_FLAG_INPUT_BF16 32u
 #define HDB_FLAG_INPUT_F16 64u
 #define HDB_FLAG_L2_NORMALIZE 128u
+/* Test only (no reference counterpart): in windows run on a thread-block
+ * cluster the first window ticket is never broadcast, so every CTA's first
+ * bounded wait runs out after 1 ms; the kernel then ends with
+ * HDB_STATUS_INTERNAL and writes no labels.  It exercises the give-up path of
+ * the cluster waits without any transfer in flight. */
+#define HDB_FLAG_TEST_STALL 256u
 
 typedef struct hdb_plan hdb_plan_t;
 
@@ -96,6 +115,12 @@ typedef struct hdb_exports {
     int64_t* stage_ns;     /* [B,8] device timestamps (ns) per window: start, Prim start, Prim end,
                                     hierarchy start, sort end, linkage end, condensation end, labels end */
     void* probabilities;   /* [T]   membership strength in [0, 1] (Real), scikit-learn's probabilities_ */
+    /* Condensed-tree rows as scikit-learn's condensed_tree_ holds them
+     * (sklearn/cluster/_hdbscan/_tree.pyx:122-237): cluster c > n_w is the row
+     * (cl_parent, c, cl_birth, cl_size); point i is (point_parent, i,
+     * point_lambda, 1). */
+    int32_t* cl_size;      /* [T]   points in each condensed cluster when it is born (root: n_w) */
+    void* point_lambda;    /* [T]   lambda at which each point falls out of its cluster (Real) */
 } hdb_exports_t;
 
 /* Library version (HDB_VERSION). */
@@ -146,6 +171,23 @@ int hdb_plan_describe(const hdb_plan_t* plan, char* buffer, size_t size);
 int hdb_plan_forward(hdb_plan_t* plan, const void* X, int32_t* labels, void* workspace, size_t workspace_bytes,
                      int32_t* status, const hdb_exports_t* exports, void* stream);
 
+/* Phases of the forward, for hdb_plan_profile. */
+#define HDB_PHASE_PREPARE 0  /* producer stage (bfloat16/float16 input, L2 normalisation) */
+#define HDB_PHASE_DISTANCE 1 /* distance blocks of matrix-variant windows */
+#define HDB_PHASE_CORE 2     /* core distances */
+#define HDB_PHASE_FORWARD 3  /* persistent Prim + hierarchy kernels */
+#define HDB_PHASES 4
+
+/* hdb_plan_forward with every launch serialized on `stream` and timed by CUDA
+ * events (no reference counterpart: the reference's stage profiler times its
+ * stages with host synchronizations, scripts/profile_cuda.py:49-90).  Writes
+ * the summed milliseconds per phase into phase_ms[HDB_PHASES] and, when not
+ * NULL, the launches per phase into phase_launches[HDB_PHASES]; synchronizes
+ * the stream.  Results equal hdb_plan_forward's. */
+int hdb_plan_profile(hdb_plan_t* plan, const void* X, int32_t* labels, void* workspace, size_t workspace_bytes,
+                     int32_t* status, const hdb_exports_t* exports, void* stream, double* phase_ms,
+                     int32_t* phase_launches);
+
 /* Capture hdb_plan_forward with these exact pointers into a CUDA graph owned
  * by the plan (replacing any previous one), then hdb_plan_replay() launches
  * it.  The pointers must stay valid while the graph is used. */
@@ -182,10 +224,13 @@ int hdb_cluster_f64(const double* X, int batch, int n, int dims, int min_cluster
  * HDB_NOALLOC_SCRATCH_BYTES compiled into this library, which stays resident
  * on every device that loads the library until the process exits.
  *  - Limits: batch <= HDB_NOALLOC_MAX_WINDOWS, batch*n <= HDB_NOALLOC_MAX_POINTS,
- *    dims <= 32 (float32) / 16 (float64); larger requests fail with
- *    HDB_E_INVALID and a message naming the limit.
- *  - The first call on a device looks up the array's device address with that
- *    device current; make that first call before any stream capture.
+ *    and dims by window size (every window's coordinates stay in registers):
+ *      float32: n <= 1024: dims <= 32; n <= 2048: dims <= 16; n <= 4096: dims <= 8
+ *      float64: n <= 1024: dims <= 16; n <= 2048: dims <= 8; larger windows: none
+ *    Larger requests fail with HDB_E_INVALID and a message naming the limit.
+ *  - The first call in a CUDA context (normally the device's primary context)
+ *    looks up the array's device address with that context current and caches
+ *    it per context; make that first call before any stream capture.
  *  - All calls share the one array and overwrite it: calls that overlap on the
  *    GPU (other streams or host threads) race; order them on one stream.
  *  - Calls no cudaMalloc/cudaFree and no allocating library routine. */
