@@ -12,11 +12,19 @@ A step = one pass of the whole pipeline over the batch:
          forward, the status read and D2H of the labels inside the timing.
 Also reported: the plain per-window launch of the same kernels (one launch per
 window, no graph), labels bit-exact against the graph run and the oracle,
-the forward kernel's roofline, and the CPU oracle on the host cores.
+float32 agreement with the float64 oracle, per-phase device times (distance
+and core phases as achieved GB/s against the measured HBM peak, Prim as ns per
+iteration, hierarchy stages in us), the forward kernel's roofline, and the CPU
+baselines: scikit-learn's HDBSCAN in a spawn process pool (one process per
+host core) where scikit-learn is installed, and the oracle restatement on all
+host threads.
 
 `--impl reference` times the reference's own kernel code compiled for the CPU
 (oracle/_ref) or, if that is absent, the oracle restatement, on all host
 threads, same workload/metric.
+
+`--gpus N` without a torchrun environment starts N ranks itself (torchrun on
+127.0.0.1); each rank clusters its own shard (weak scaling).
 """
 
 from __future__ import annotations
@@ -27,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -60,11 +69,10 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"hdbscan_gb300_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.file = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -99,6 +107,10 @@ class ClockSampler:
             for name, flag in zip(names, parts[5:9]):
                 if flag.lower() == "active":
                     reasons.add(name)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
@@ -142,6 +154,100 @@ def cpu_reference_batch(packed, offsets, params, threads, prefer_reference=True)
 def sample_windows(offsets, target_windows):
     count = min(len(offsets) - 1, target_windows)
     return offsets[: count + 1].copy(), count
+
+
+# scikit-learn runs with the scalar NumPy sort on x86 (its AVX2/AVX-512 argsort
+# orders ties differently from the reference's introsort) and one BLAS thread.
+SCALAR_SORT_ENV = {"NPY_DISABLE_CPU_FEATURES": "X86_V3 X86_V4 AVX512_ICL AVX512_SPR"}
+ONE_THREAD_ENV = {"OMP_NUM_THREADS": "1", "OPENBLAS_NUM_THREADS": "1", "MKL_NUM_THREADS": "1"}
+
+
+def _sklearn_fit(job):
+    x, mcs, ms, eps = job
+    from sklearn.cluster import HDBSCAN
+
+    model = HDBSCAN(algorithm="auto", metric="euclidean", cluster_selection_method="eom", allow_single_cluster=False,
+                    alpha=1.0, n_jobs=1, copy=True, min_cluster_size=mcs, min_samples=ms, cluster_selection_epsilon=eps)
+    return model.fit_predict(x).astype(np.int32)
+
+
+def _sklearn_worker_ready(pause):
+    import sklearn
+    from sklearn.cluster import HDBSCAN  # noqa: F401  (imported before the timing)
+
+    time.sleep(pause)  # hold this worker so every worker takes one warm-up task
+    return sklearn.__version__, np.__version__, os.environ.get("NPY_DISABLE_CPU_FEATURES", "")
+
+
+def sklearn_baseline(packed, offsets, params, count):
+    """scikit-learn's HDBSCAN, the reference's CPU comparison (benchmarks/benchmark.py:90-94 there), on
+    the first `count` windows: a persistent spawn process pool, one single-threaded process per host
+    core, every worker started and warmed before the timing (the reference's start barrier,
+    benchmarks/benchmark.py:222-238 there).  Float32 configurations give scikit-learn the
+    float32-rounded points (it computes in float64)."""
+    import importlib.util
+    import multiprocessing
+    import platform
+    from concurrent.futures import ProcessPoolExecutor
+
+    if importlib.util.find_spec("sklearn") is None:
+        return {"unavailable": "scikit-learn is not installed on this host"}
+    cores = len(os.sched_getaffinity(0))
+    env = dict(ONE_THREAD_ENV)
+    if platform.machine().lower() in ("x86_64", "amd64"):
+        env.update(SCALAR_SORT_ENV)
+    saved = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)  # inherited by the spawned workers
+    try:
+        pool = ProcessPoolExecutor(cores, mp_context=multiprocessing.get_context("spawn"))
+        versions = list(pool.map(_sklearn_worker_ready, [0.5] * cores))[0]
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    mcs, ms, eps = params["min_cluster_size"], params["min_samples"], params["cluster_selection_epsilon"]
+    x = packed if params["precision"] == "float64" else packed.astype(np.float32).astype(np.float64)
+    jobs = [(np.ascontiguousarray(x[int(offsets[w]):int(offsets[w + 1])]), mcs, ms, eps) for w in range(count)]
+    with pool:
+        t0 = time.perf_counter()
+        labels = list(pool.map(_sklearn_fit, jobs))
+        elapsed = time.perf_counter() - t0
+    return {"value": count / elapsed, "unit": "windows/s", "cores": cores, "kind": "sklearn",
+            "sample": f"first {count} windows, {cores} spawn processes x 1 thread",
+            "versions": {"sklearn": versions[0], "numpy": versions[1], "NPY_DISABLE_CPU_FEATURES": versions[2]},
+            "labels": labels}
+
+
+def phase_report(phase_ms, phase_launches, describe, D, itemsize, peak, core_distances):
+    """Distance and core phases as achieved GB/s of algorithmic bytes (against the HBM peak), the
+    forward as device ms.  Algorithmic bytes (sums over the windows of each kind):
+      distance: read X (n*D*s) + write the n x n block (n^2*s), matrix-variant windows;
+      core:     matrix windows read their block (n^2*s) + write core and neighbour (n*(s+4));
+                recompute windows read X (n*D*s) + the same writes (these are SIMT-bound)."""
+    matrix = [c for c in describe["classes"] if c["variant"] == "matrix"]
+    recompute = [c for c in describe["classes"] if c["variant"] != "matrix"]
+    points_m = sum(c["points"] for c in matrix)
+    n2_m = sum(c["sum_n2"] for c in matrix)
+    points_r = sum(c["points"] for c in recompute)
+    out = {}
+    dist_bytes = (n2_m + points_m * D) * itemsize
+    if phase_launches["distance"]:
+        gbs = dist_bytes / (phase_ms["distance"] / 1e3) / 1e9
+        out["distance"] = {"ms": phase_ms["distance"], "launches": phase_launches["distance"], "bytes": dist_bytes,
+                           "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+    if core_distances and phase_launches["core"]:
+        core_bytes = n2_m * itemsize + (points_m + points_r) * (itemsize + 4) + points_r * D * itemsize
+        gbs = core_bytes / (phase_ms["core"] / 1e3) / 1e9
+        out["core"] = {"ms": phase_ms["core"], "launches": phase_launches["core"], "bytes": core_bytes,
+                       "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+    if phase_launches["prepare"]:
+        out["prepare"] = {"ms": phase_ms["prepare"], "launches": phase_launches["prepare"]}
+    out["forward"] = {"ms": phase_ms["forward"], "launches": phase_launches["forward"],
+                      "note": "persistent Prim + hierarchy kernels: latency-bound, see stages"}
+    out["note"] = "every launch serialized on one stream and event-timed (the graph overlaps them)"
+    return out
 
 
 def run_reference_arm(args, packed, offsets, params):
@@ -204,6 +310,19 @@ def whole_job_rate(windows_per_rank, world, ms_per_step):
     return windows_per_rank * world / (ms_per_step / 1e3)
 
 
+def launch_ranks(gpus):
+    """Start `gpus` ranks of this command under torchrun on 127.0.0.1 (one process per GPU); returns
+    torchrun's exit status.  Rank 0 prints the JSON line."""
+    import socket
+
+    with socket.socket() as probe:
+        probe.bind(("127.0.0.1", 0))
+        port = probe.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     parser = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     parser.add_argument("--gpus", type=int, default=1)
@@ -216,7 +335,9 @@ def main():
     parser.add_argument("--skip-cpu", action="store_true")
     parser.add_argument("--windows", type=int, default=None,
                         help="override the config's window count (small cases for ncu captures)")
-    parser.add_argument("--stages", action="store_true", help="report per-stage device time of the forward kernel")
+    parser.add_argument("--stages", action="store_true", help="(always on) per-stage device time of the forward")
+    parser.add_argument("--sklearn-windows", type=int, default=256,
+                        help="windows of the scikit-learn CPU baseline sample (where scikit-learn is installed)")
     parser.add_argument("--backward", choices=("auto", "on", "off"), default="auto",
                         help="time forward+backward (default: on for the c4/c5 differentiation configs)")
     parser.add_argument("--profile", action="store_true",
@@ -224,6 +345,8 @@ def main():
     args = parser.parse_args()
     if args.warmup < 3:
         parser.error("--warmup must be >= 3")
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus))
 
     rank, world, local = dist_env()
     packed64, offsets, params = rank_workload(args.config, rank, args.windows)
@@ -301,33 +424,28 @@ def main():
     ms_per_step = reduce_max(float(np.mean(step_ms)), world, device)
     value = whole_job_rate(B, world, ms_per_step)
 
-    # ---- kernel-only timing of the forward kernel (non-graph launch) --------
-    kernel_ms = []
-    for _ in range(max(3, args.steps // 2)):
+    # ---- per-phase device time: every launch serialized and event-timed ------
+    # (hdb_plan_profile), with globaltimer stamps per window inside the forward.
+    profiles = []
+    stamps = torch.zeros((B, 8), dtype=torch.int64, device=device)
+    for i in range(3):
         flush.fill_(1)
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        plan.forward(X, labels=labels, workspace=workspace, status=status)
-        end.record(stream)
-        end.synchronize()
-        kernel_ms.append(start.elapsed_time(end))
-    kernel_ms_mean = float(np.mean(kernel_ms))
-
-    # ---- per-stage device time (globaltimer stamps inside the kernel) -------
-    stages = None
-    if args.stages:
-        stamps = torch.zeros((B, 8), dtype=torch.int64, device=device)
-        plan.forward(X, labels=labels, workspace=workspace, status=status, exports={"stage_ns": stamps})
-        torch.cuda.synchronize()
-        st = stamps.cpu().numpy().astype(np.float64)
-        names = ["stage", "prim", "handoff_wait", "sort", "linkage", "condense", "select_label"]
-        dur = np.diff(st, axis=1) / 1e3
-        stages = {name: {"median_us": float(np.median(dur[:, i])), "max_us": float(dur[:, i].max())}
-                  for i, name in enumerate(names)}
-        stages["window_total_us"] = {"median_us": float(np.median(st[:, 7] - st[:, 0]) / 1e3),
-                                     "max_us": float((st[:, 7] - st[:, 0]).max() / 1e3)}
-        n_med = float(np.median(np.diff(offsets)))
-        stages["prim_ns_per_iteration"] = float(np.median(dur[:, 1]) * 1e3 / max(n_med - 1, 1))
+        profiles.append(plan.profile(X, labels=labels, workspace=workspace, status=status,
+                                     exports={"stage_ns": stamps} if i == 0 else None))
+    raise_for_status(int(status.item()))
+    phase_ms = {name: float(np.mean([pr[name][0] for pr in profiles])) for name in _lib.PHASES}
+    phase_launches = {name: profiles[0][name][1] for name in _lib.PHASES}
+    kernel_ms_mean = phase_ms["forward"]
+    st = stamps.cpu().numpy().astype(np.float64)
+    stage_names = ["stage", "prim", "handoff_wait", "sort", "linkage", "condense", "select_label"]
+    dur = np.diff(st, axis=1) / 1e3
+    stages = {name: {"median_us": float(np.median(dur[:, i])), "max_us": float(dur[:, i].max())}
+              for i, name in enumerate(stage_names)}
+    sizes = np.diff(offsets)
+    per_iter = dur[:, 1] * 1e3 / np.maximum(sizes - 1, 1)
+    stages["prim_ns_per_iteration"] = {"median": float(np.median(per_iter)),
+                                       "largest_window": float(per_iter[int(np.argmax(sizes))])}
+    stages["note"] = "per window, from the serialized profile run (globaltimer stamps)"
 
     # ---- plain per-window launches of the same kernels ----------------------
     plain_plans = {}
@@ -397,8 +515,10 @@ def main():
     e2e_exact = bool(np.array_equal(out.numpy().reshape(-1), graph_labels))
     e2e_value = whole_job_rate(B, world, reduce_max(float(np.median(e2e_ms)), world, device))
 
-    # ---- oracle parity on a sample + CPU baseline ---------------------------
+    # ---- checks after the timing: oracle parity on a sample, float32 vs the --
+    # float64 oracle (the checker in float64 on the same float32-rounded input)
     from oracle import oracle
+    from tests.conftest import partition_equal
 
     sample = list(range(0, B, max(1, B // 8)))[:8]
     oracle_exact = True
@@ -406,7 +526,29 @@ def main():
         lo, hi = int(offsets[w]), int(offsets[w + 1])
         o = oracle.cluster(host[lo:hi], mcs, ms, eps, precision)
         oracle_exact &= bool(np.array_equal(o["labels"], graph_labels[lo:hi]))
+    agreement = None
+    if precision == "float32":
+        count = min(B, 64)
+        sub = offsets[:count + 1]
+        want = oracle.batch_ex(host[:int(sub[-1])].astype(np.float64), sub, mcs, ms, eps, "float64")
+        check_exports = plan.export_buffers(hierarchy=False, gradients=True)
+        plan.forward(X, labels=labels, workspace=workspace, status=status, exports=check_exports)
+        got_w = check_exports["link_w"].cpu().numpy()
+        torch.cuda.synchronize()
+        exact, worst = 0, 0.0
+        for w in range(count):
+            lo, hi = int(sub[w]), int(sub[w + 1])
+            exact += partition_equal(graph_labels[lo:hi], want["labels"][lo:hi])
+            a = np.sort(got_w[lo - w:hi - w - 1].astype(np.float64))
+            b = np.sort(want["link_w"][lo - w:hi - w - 1])
+            worst = max(worst, float(np.max(np.abs(a - b) / np.maximum(np.abs(b), np.finfo(np.float64).tiny))))
+        agreement = {"windows": count, "exact_partitions": exact, "exact_partition_rate": exact / count,
+                     "max_rel_merge_weight_error": worst,
+                     "against": "float64 oracle on the same float32-rounded input (first windows)"}
+
+    # ---- CPU baselines (rank 0): scikit-learn in a spawn pool, oracle port ---
     cpu = None
+    cpu_port = None
     if not args.skip_cpu and rank == 0:
         threads = len(os.sched_getaffinity(0))
         sub_offsets, count = sample_windows(offsets, args.cpu_windows)
@@ -414,29 +556,34 @@ def main():
         _, kind = cpu_reference_batch(host[: int(sub_offsets[-1])], sub_offsets, params, threads,
                                       prefer_reference=False)
         elapsed = time.perf_counter() - t0
-        cpu = {"value": count / elapsed, "unit": "windows/s", "cores": threads, "kind": kind,
-               "sample": f"first {count} of {B} windows, oracle restatement on {threads} host threads"}
+        cpu_port = {"value": count / elapsed, "unit": "windows/s", "cores": threads, "kind": kind,
+                    "sample": f"first {count} of {B} windows, oracle restatement on {threads} host threads"}
+        sk = sklearn_baseline(host.astype(np.float64), offsets, params, min(count, args.sklearn_windows))
+        if "labels" in sk:
+            got = [graph_labels[int(offsets[w]):int(offsets[w + 1])] for w in range(len(sk["labels"]))]
+            sk["exact_partition_rate_vs_ours"] = float(np.mean([partition_equal(g, l)
+                                                                for g, l in zip(got, sk.pop("labels"))]))
+            cpu = sk
+        else:
+            cpu = dict(cpu_port, sklearn=sk)
 
     # ---- roofline of the forward kernel -------------------------------------
     peak, peak_kind = load_peaks()
     itemsize = 4 if precision == "float32" else 8
     sizes = np.diff(offsets)
     describe = json.loads(plan.describe())
-    matrix = any(c["variant"] == "matrix" for c in describe["classes"])
     # Algorithmic bytes per launch: read X (N*D*s) + write labels (4N) per window,
-    # plus the N^2*s distance block read when the matrix variant is used.
+    # plus the N^2*s distance block read by windows of the matrix variant.
     algo_bytes = float(np.sum(sizes * D * itemsize + sizes * 4))
-    if matrix:
-        algo_bytes += float(np.sum(sizes.astype(np.float64) ** 2 * itemsize))
+    algo_bytes += float(sum(c["sum_n2"] for c in describe["classes"] if c["variant"] == "matrix") * itemsize)
     achieved = algo_bytes / (kernel_ms_mean / 1e3) / 1e9
     traffic = None
     traffic_path = ROOT / "profiles" / f"traffic_{args.config}.json"
     if traffic_path.exists():
         traffic = json.loads(traffic_path.read_text()).get("dram_bytes_per_launch")
-    launches_per_step = (len(describe["classes"]) + len(describe["core"]) +
-                         sum(1 for c in describe["classes"] if c["distance_tiles"]))
+    launches_per_step = sum(phase_launches.values())  # this library's kernels in one forward
     if backward:
-        launches_per_step += 2  # dX zeroing + backward kernel
+        launches_per_step += 1  # the backward kernel (dX is zeroed by torch)
     line = {
         "metric": "windows_per_s", "value": value, "unit": "windows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -454,8 +601,12 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "hdb_forward_kernel", "kernel_ms": kernel_ms_mean,
-                     "note": "latency-bound (serial Prim/tree chains); algorithmic bytes per launch"},
+                     "note": "latency-bound (serial Prim/tree chains); algorithmic bytes per launch over the "
+                             "forward kernels' event-timed duration"},
         "cpu_baseline": cpu,
+        "cpu_baseline_port": cpu_port,
+        "float32_vs_float64_oracle": agreement,
+        "phases": phase_report(phase_ms, phase_launches, describe, D, itemsize, peak, ms > 2),
         "stages": stages,
         "clocks": clocks.summary(),
         "plan": describe["classes"],

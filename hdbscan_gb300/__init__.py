@@ -9,7 +9,7 @@ hierarchy exports and differentiable merge weights (``merge_weights``).
 
 from ._api import MAX_SAMPLES, hdbscan
 
-__all__ = ["hdbscan", "hdbscan_ragged", "Plan", "merge_weights", "MAX_SAMPLES"]
+__all__ = ["hdbscan", "hdbscan_ragged", "condensed_tree", "Plan", "merge_weights", "MAX_SAMPLES"]
 
 
 def __getattr__(name):
@@ -22,6 +22,10 @@ def __getattr__(name):
         from ._ragged import hdbscan_ragged
 
         return hdbscan_ragged
+    if name == "condensed_tree":
+        from ._ragged import condensed_tree
+
+        return condensed_tree
     if name == "merge_weights":
         from ._autograd import merge_weights
 

@@ -59,9 +59,10 @@ def merge_weights(X, offsets=None, *, min_cluster_size=5, min_samples=None, clus
         offsets = np.arange(batch + 1, dtype=np.int64) * n
         packed = X.reshape(batch * n, shape[-1])
     else:
+        if X.ndim != 2:
+            raise ValueError("with offsets, X must be the packed [T, D] windows")
         offsets = np.asarray(offsets, dtype=np.int64)
         packed = X
-        n = int(np.diff(offsets).max())
     sizes = np.diff(offsets)
     validate_limits(int(sizes.max()), min_cluster_size, min_samples, cluster_selection_epsilon, precision)
     if min_samples > int(sizes.min()):
@@ -72,8 +73,6 @@ def merge_weights(X, offsets=None, *, min_cluster_size=5, min_samples=None, clus
         plan = plan_for(offsets, packed.shape[1], min_cluster_size, min_samples, cluster_selection_epsilon,
                         precision, force_matrix)
         weights, labels = _MergeWeights.apply(packed.contiguous(), plan)
-    if X.ndim == 3 and len(offsets) - 1 == shape[0] and offsets is not None and X.shape[0] * X.shape[1] == packed.shape[0]:
+    if X.ndim == 3:  # dense [B, N, D]: one row of merge weights / labels per window
         return weights.view(shape[0], shape[1] - 1), labels.view(shape[0], shape[1])
-    if X.ndim == 2 and len(offsets) == 2:
-        return weights, labels
     return weights, labels

@@ -53,7 +53,7 @@ class Plan:
 
     def __init__(self, offsets, dims, *, min_cluster_size=5, min_samples=None, cluster_selection_epsilon=0.0,
                  precision="float32", force_matrix=False, one_persistent=False, cluster_selection_method="eom",
-                 allow_single_cluster=False, input_dtype=None, normalize=False, device=None):
+                 allow_single_cluster=False, input_dtype=None, normalize=False, device=None, test_flags=0):
         if precision not in _DTYPES:
             raise ValueError("precision must be 'float32' or 'float64'")
         _require_gpu()
@@ -77,7 +77,7 @@ class Plan:
             _lib.HDB_FLAG_ONE_PERSISTENT if one_persistent else 0) | (
             _lib.HDB_FLAG_LEAF if cluster_selection_method == "leaf" else 0) | (
             _lib.HDB_FLAG_ALLOW_SINGLE if allow_single_cluster else 0) | (
-            _HALF_INPUTS.get(input_dtype, 0)) | (_lib.HDB_FLAG_L2_NORMALIZE if normalize else 0)
+            _HALF_INPUTS.get(input_dtype, 0)) | (_lib.HDB_FLAG_L2_NORMALIZE if normalize else 0) | int(test_flags)
         if input_dtype is not None and input_dtype not in _HALF_INPUTS and input_dtype != self.torch_dtype:
             raise ValueError("input_dtype must be torch.bfloat16, torch.float16 or the compute precision")
         self.input_dtype = self.torch_dtype if input_dtype is None else input_dtype
@@ -135,6 +135,8 @@ class Plan:
                 cl_stability=torch.empty(T, dtype=dt, device=dev),
                 cl_selected=torch.empty(T, dtype=torch.uint8, device=dev),
                 point_parent=torch.empty(T, dtype=torch.int32, device=dev),
+                cl_size=torch.empty(T, dtype=torch.int32, device=dev),
+                point_lambda=torch.empty(T, dtype=dt, device=dev),
             )
         if self.min_samples > 2:
             out.update(core=torch.empty(T, dtype=dt, device=dev),
@@ -170,6 +172,23 @@ class Plan:
                 status.data_ptr(), ctypes.byref(ex) if ex is not None else None, _stream_handle(self.device)),
                 "hdb_plan_forward")
         return labels, status
+
+    def profile(self, X, labels=None, workspace=None, status=None, exports=None):
+        """The forward with every launch serialized and timed by CUDA events (synchronizes).
+        Returns {phase: (milliseconds, launches)} for prepare/distance/core/forward."""
+        X = self._check_x(X)
+        labels = torch.empty(self.points, dtype=torch.int32, device=self.device) if labels is None else labels
+        workspace = self.workspace() if workspace is None else workspace
+        status = torch.empty(1, dtype=torch.int32, device=self.device) if status is None else status
+        ex = self._exports_struct(exports)
+        ms = (ctypes.c_double * len(_lib.PHASES))()
+        launches = (ctypes.c_int32 * len(_lib.PHASES))()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().hdb_plan_profile(
+                self._handle, X.data_ptr(), labels.data_ptr(), workspace.data_ptr(), workspace.numel(),
+                status.data_ptr(), ctypes.byref(ex) if ex is not None else None, _stream_handle(self.device),
+                ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(launches, ctypes.c_void_p)), "hdb_plan_profile")
+        return {name: (float(ms[i]), int(launches[i])) for i, name in enumerate(_lib.PHASES)}
 
     def capture(self, X, labels=None, workspace=None, status=None, exports=None):
         """Capture the forward for these buffers into a CUDA graph; returns (labels, status)."""

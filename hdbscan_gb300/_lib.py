@@ -21,9 +21,11 @@ HDB_FLAG_ALLOW_SINGLE = 16
 HDB_FLAG_INPUT_BF16 = 32
 HDB_FLAG_INPUT_F16 = 64
 HDB_FLAG_L2_NORMALIZE = 128
+HDB_FLAG_TEST_STALL = 256
 STATUS_OVERFLOW = 1
 STATUS_NONFINITE = 2
 STATUS_INTERNAL = 4
+PHASES = ("prepare", "distance", "core", "forward")
 
 _P = ctypes.c_void_p
 _lock = threading.Lock()
@@ -31,7 +33,7 @@ _lib = None
 
 EXPORT_FIELDS = ("edges_uv", "edge_w", "order", "link_lr", "link_w", "link_size", "n_clusters", "cl_parent",
                  "cl_birth", "cl_stability", "cl_selected", "point_parent", "core", "core_nbr", "stage_ns",
-                 "probabilities")
+                 "probabilities", "cl_size", "point_lambda")
 
 
 class Exports(ctypes.Structure):
@@ -59,6 +61,8 @@ def _declare(handle):
         "hdb_plan_forward": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_size_t, _P, ctypes.POINTER(Exports), _P]),
         "hdb_plan_capture": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_size_t, _P, ctypes.POINTER(Exports), _P]),
         "hdb_plan_replay": (ctypes.c_int, [_P, _P]),
+        "hdb_plan_profile": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_size_t, _P, ctypes.POINTER(Exports), _P, _P,
+                                            _P]),
         "hdb_plan_backward": (ctypes.c_int, [_P, _P, ctypes.POINTER(Exports), _P, _P, _P, ctypes.c_size_t, _P]),
         "hdb_cluster_workspace_bytes": (ctypes.c_size_t, [ctypes.c_int] * 6),
         "hdb_cluster_f32": (ctypes.c_int, [_P] + [ctypes.c_int] * 5 + [ctypes.c_double, _P, _P, ctypes.c_size_t,
@@ -78,7 +82,8 @@ def _declare(handle):
 # Every symbol include/hdbscan_gb300.h declares.
 SYMBOLS = ("hdb_version", "hdb_last_error", "hdb_set_tuning", "hdb_get_tuning", "hdb_list_variants",
            "hdb_plan_create", "hdb_plan_destroy", "hdb_plan_workspace_bytes",
-           "hdb_plan_describe", "hdb_plan_forward", "hdb_plan_capture", "hdb_plan_replay", "hdb_plan_backward",
+           "hdb_plan_describe", "hdb_plan_forward", "hdb_plan_profile", "hdb_plan_capture", "hdb_plan_replay",
+           "hdb_plan_backward",
            "hdb_cluster_workspace_bytes", "hdb_cluster_f32", "hdb_cluster_f64", "hdb_cluster_noalloc")
 
 

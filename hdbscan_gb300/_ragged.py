@@ -50,3 +50,33 @@ def hdbscan_ragged(windows=None, *, packed=None, offsets=None, min_cluster_size=
         labels, exports = result
         return labels, offsets, exports
     return result, offsets
+
+
+def condensed_tree(hierarchy, offsets):
+    """Per-window condensed trees in scikit-learn's ``condensed_tree_`` columns.
+
+    `hierarchy` is the dict hdbscan_ragged(..., return_hierarchy=True) returns.
+    For each window, a dict of device tensors ``parent``, ``child``,
+    ``lambda_val`` and ``child_size`` (sklearn/cluster/_hdbscan/_tree.pyx:
+    122-237): one row per point (child = point index, size 1) followed by one
+    row per condensed cluster except the root (child = cluster id >= n + 1),
+    ordered by child.  Only the per-window cluster counts are read back.
+    """
+    import torch
+
+    offsets = np.asarray(offsets, dtype=np.int64)
+    counts = hierarchy["n_clusters"].cpu().numpy()
+    device = hierarchy["point_parent"].device
+    trees = []
+    for w in range(len(offsets) - 1):
+        lo, hi = int(offsets[w]), int(offsets[w + 1])
+        n, k = hi - lo, int(counts[w])
+        clusters = slice(lo + 1, lo + k)  # row c - n of cluster c; the root (c = n) has no row
+        trees.append({
+            "parent": torch.cat([hierarchy["point_parent"][lo:hi], hierarchy["cl_parent"][clusters]]),
+            "child": torch.arange(n + k, dtype=torch.int32, device=device)[torch.arange(n + k, device=device) != n],
+            "lambda_val": torch.cat([hierarchy["point_lambda"][lo:hi], hierarchy["cl_birth"][clusters]]),
+            "child_size": torch.cat([torch.ones(n, dtype=torch.int32, device=device),
+                                     hierarchy["cl_size"][clusters]]),
+        })
+    return trees

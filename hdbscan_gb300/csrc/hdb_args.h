@@ -47,8 +47,15 @@ struct ForwardArgs {
     int32_t* point_parent;     // [T]
     int64_t* stage_ns;         // [B, 8] globaltimer at stage boundaries (diagnostics)
     void* probabilities;       // [T] membership strengths (Real)
+    int32_t* cl_size;          // [T] cluster sizes at birth
+    void* point_lambda;        // [T] lambda at which each point falls out (Real)
     int method;                // cluster selection: 0 excess of mass, 1 leaf
     int allow_single;          // the root may be selected
+    // Cluster form only: limit of every bounded mbarrier wait (0 = the 2 s
+    // default), and a test switch under which the first window ticket is never
+    // broadcast, so every CTA's first wait runs out (nothing is in flight then).
+    int64_t wait_limit_ns;
+    int stall_first_ticket;
 };
 
 struct DistanceArgs {

@@ -124,9 +124,11 @@ __device__ __forceinline__ void cluster_barrier() {
 
 constexpr int64_t kWaitLimitNs = 2000000000ll;  // 2 s: far above any legitimate wait
 
-// Bounded wait for the completion of phase `parity` of a local mbarrier.
-// Returns false when this wait or an earlier one of the CTA gave up.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+// Bounded wait for the completion of phase `parity` of a local mbarrier, for
+// at most `limit_ns` of %globaltimer (and 2^30 polls).  Returns false when
+// this wait or an earlier one of the CTA gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          int64_t limit_ns) {
     if (mbar_test(bar, parity)) return true;
     if (*abort_flag) return false;
     const int64_t t0 = global_ns();
@@ -134,7 +136,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
         if (mbar_test(bar, parity)) return true;
         if ((spin & 31) == 31) {
             if (*abort_flag) return false;
-            if (global_ns() - t0 > kWaitLimitNs) break;
+            if (global_ns() - t0 > limit_ns) break;
         }
     }
     *abort_flag = 1;
@@ -213,6 +215,7 @@ struct ClusterShared {
     unsigned char* recs_ptr;
     unsigned char* rec0;  // local record of vertex 0 (first current vertex)
     volatile int* abort_flag;
+    int64_t wait_limit;   // ns, every mbarrier wait
     int* vflags;          // this window's validation flags
     int* oflags;          // this window's overflow flags
     int* xc_out;
@@ -228,7 +231,7 @@ __device__ __forceinline__ int exchange_flags(const ClusterShared& cs, uint32_t 
     send_record<Real, DP, CS, 0>(slot, cs.full0 + 8 * p, rank, (typename RealTraits<Real>::Bits)0, 0u,
                                  (uint32_t)flags, Real(0), nullptr);
     int all = 0;
-    if (!mbar_wait(cs.full0 + 8 * p, ph, cs.abort_flag)) all |= 4;
+    if (!mbar_wait(cs.full0 + 8 * p, ph, cs.abort_flag, cs.wait_limit)) all |= 4;
 #pragma unroll
     for (int r = 0; r < CS; ++r) {
         const unsigned char* rp = cs.recs_ptr + (p * CS + r) * Rec::kBytes;
@@ -459,7 +462,7 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
                 send_record<Real, DP, CS, 0>(slot, cs.full0 + 8 * p, rank, SENTINEL, 0xffffffffu, 0u, Real(0),
                                              nullptr);
             }
-            if (!mbar_wait(cs.full0 + 8 * p, ph, cs.abort_flag)) overflow |= 4;
+            if (!mbar_wait(cs.full0 + 8 * p, ph, cs.abort_flag, cs.wait_limit)) overflow |= 4;
             Key wk = SENTINEL;
             uint32_t wv = 0xffffffffu;
             int wr = 0;
@@ -536,6 +539,7 @@ __global__ void __launch_bounds__(PT + 32, 1) hdb_cluster_forward_kernel(const _
     cs.rec0 = cs.recs_ptr + 2 * CS * Rec::kBytes;
     cs.full0 = smem_u32(&s_full[0]);
     cs.abort_flag = &s_abort;
+    cs.wait_limit = args.wait_limit_ns > 0 ? args.wait_limit_ns : kWaitLimitNs;
     cs.vflags = &s_vflags[0];
     cs.oflags = &s_oflags[0];
     cs.xc_out = &s_xc;
@@ -571,7 +575,7 @@ __global__ void __launch_bounds__(PT + 32, 1) hdb_cluster_forward_kernel(const _
     uint32_t xc = 0;  // exchange counter, identical in every CTA of the cluster
     int homes = 0;
     for (int k = 0; k < (1 << 30); ++k) {
-        if (rank == 0 && tid == 0) {
+        if (rank == 0 && tid == 0 && !(args.stall_first_ticket && k == 0)) {
             const int item = s_abort ? args.queue_len : atomicAdd(args.ticket, 1);
 #pragma unroll
             for (uint32_t r = 0; r < (uint32_t)CS; ++r) {
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(PT + 32, 1) hdb_cluster_forward_kernel(const _
             }
         }
         if (tid == 0) {
-            if (!mbar_wait(smem_u32(&s_item_bar), k & 1, &s_abort)) {
+            if (!mbar_wait(smem_u32(&s_item_bar), k & 1, &s_abort, cs.wait_limit)) {
                 atomic_status(args.status, kInternal);
                 s_item[k & 1] = args.queue_len;
             }

@@ -358,8 +358,12 @@ __device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char*
         }
     }
     __syncwarp();
-    const int next_label = condense_warp<Real>(a, n, args.mcs);
+    const int next_label = condense_warp<Real>(a, n, args.mcs, args.cl_size ? args.cl_size + base : nullptr);
     if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 6] = global_ns();
+    if (args.point_lambda) {  // s8: the linkage node each point was pruned at; r0: lambda per node
+        Real* out = static_cast<Real*>(args.point_lambda) + base;
+        for (int i = lane; i < n; i += 32) out[i] = a.r0[a.s8[i] - n];
+    }
     if (args.cl_parent) {
         for (int c = lane; c < next_label - n; c += 32) {
             args.cl_parent[base + c] = a.s2[c];

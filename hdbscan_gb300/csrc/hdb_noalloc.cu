@@ -12,11 +12,17 @@
 // __device__ array of kScratchBytes, resident on every device that loads this
 // library until the process exits.  Host code must not use the array's name as
 // a device address (in host code it names a host-side stand-in), so the first
-// call on each device resolves the real address once with
-// cudaGetSymbolAddress, with that device current, and caches it.  That first
-// call should therefore come before any stream capture.  A small kernel
-// rebuilds the tables in the scratch on every call (nothing is copied from
-// host memory), so no pinned buffer is needed either.
+// call in each CUDA context resolves the real address with
+// cudaGetSymbolAddress, with that context's device current, and caches it
+// under the context's unique id (a context created later, for instance after
+// cudaDeviceReset, gets its own lookup).  That first call should therefore
+// come before any stream capture.  A small kernel rebuilds the tables in the
+// scratch on every call (nothing is copied from host memory), so no pinned
+// buffer is needed either.
+//
+// Limits: the Prim kernels this entry point can use keep every window's
+// coordinates in registers (no distance-block workspace), so the dims a window
+// may have shrink as its point count grows (noalloc_max_dims below).
 //
 // Every call shares the array and overwrites what the previous call left:
 // calls that overlap on the GPU (other streams, other host threads) race with
@@ -24,7 +30,9 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <vector>
 
+#include <cuda.h>  // CUcontext / CUresult types only; the driver calls are resolved at run time
 #include <cuda_runtime.h>
 
 #include "../../include/hdbscan_gb300.h"
@@ -34,7 +42,6 @@
 namespace {
 
 constexpr size_t kScratchBytes = HDB_NOALLOC_SCRATCH_BYTES;
-constexpr int kMaxDevices = 64;
 
 // Byte layout of the scratch array.
 constexpr size_t kOffOffsets = 0;                                                     // int64 [windows+1]
@@ -48,7 +55,11 @@ static_assert(kScratchUsed <= kScratchBytes, "no-allocation scratch layout excee
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_scratch_mutex;
-unsigned char* g_scratch_device[kMaxDevices] = {};
+struct ScratchEntry {
+    unsigned long long context;  // unique id of the CUDA context (cuCtxGetId), or the device ordinal
+    unsigned char* address;
+};
+std::vector<ScratchEntry> g_scratch_device;
 
 // Failures are reported through the library's hdb_last_error().
 int fail(int code, const std::string& message) {
@@ -56,20 +67,62 @@ int fail(int code, const std::string& message) {
     return code;
 }
 
-// Device address of the scratch array on `device` (which must be current).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current context, through driver entry points looked up by
+// the runtime (no link-time dependency on the driver library).  False when the
+// driver offers no such query or no context is current yet.
+bool current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult found;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &found) == cudaSuccess &&
+            found == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &found) == cudaSuccess &&
+            found == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(fn);
+    });
+    if (!get_current || !get_id) return false;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device address of the scratch array in the current context (on `device`).
 int scratch_address(int device, unsigned char** out) {
-    if (device < 0 || device >= kMaxDevices) return fail(HDB_E_DEVICE, "device index out of range");
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_device[device]) {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return fail(HDB_E_CUDA, std::string("cudaGetSymbolAddress(no-allocation scratch): ") +
-                                        cudaGetErrorString(e));
-        g_scratch_device[device] = static_cast<unsigned char*>(ptr);
-    }
-    *out = g_scratch_device[device];
+    unsigned long long key = 0;
+    const bool by_context = current_context_id(&key);
+    if (by_context) key |= 1ull << 63;  // context ids and device ordinals never collide
+    else key = (unsigned long long)device;
+    for (const ScratchEntry& e : g_scratch_device)
+        if (e.context == key) {
+            *out = e.address;
+            return HDB_OK;
+        }
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return fail(HDB_E_CUDA, std::string("cudaGetSymbolAddress(no-allocation scratch): ") + cudaGetErrorString(e));
+    // The lookup above may have created the context; key the entry on it.
+    unsigned long long now = 0;
+    if (current_context_id(&now)) key = now | (1ull << 63);
+    g_scratch_device.push_back({key, static_cast<unsigned char*>(ptr)});
+    *out = static_cast<unsigned char*>(ptr);
     return HDB_OK;
+}
+
+// Largest dims a window of n points may have in this precision (0: none): the
+// register-resident Prim variants hold slots x register dims <= 64 words.
+int noalloc_max_dims(int precision, int n) {
+    if (precision == HDB_F32) return n <= 1024 ? 32 : (n <= 2048 ? 16 : 8);
+    return n <= 1024 ? 16 : (n <= 2048 ? 8 : 0);
 }
 
 // Rebuilds the uniform-batch tables; also zeroes the ticket and the status.
@@ -140,16 +193,20 @@ extern "C" int hdb_cluster_noalloc(int precision, const void* X, int batch, int 
     if (min_samples > n) return fail(HDB_E_INVALID, "min_samples must not exceed the number of samples");
     if (!(epsilon >= 0) || epsilon > 1.7976931348623157e308)
         return fail(HDB_E_INVALID, "cluster_selection_epsilon must be finite and >= 0");
+    if (precision == HDB_F32 && epsilon > 3.4028234663852886e38)
+        return fail(HDB_E_INVALID, "cluster_selection_epsilon is not representable in the requested precision");
     if (batch > HDB_NOALLOC_MAX_WINDOWS || (int64_t)batch * n > HDB_NOALLOC_MAX_POINTS)
         return fail(HDB_E_INVALID, "batch of " + std::to_string(batch) + " x " + std::to_string(n) +
                                        " points exceeds the no-allocation limit (at most " +
                                        std::to_string(HDB_NOALLOC_MAX_WINDOWS) + " windows and " +
                                        std::to_string(HDB_NOALLOC_MAX_POINTS) + " points)");
-    const int max_dims = precision == HDB_F32 ? 32 : 16;
+    const int max_dims = noalloc_max_dims(precision, n);
     if (dims > max_dims)
-        return fail(HDB_E_INVALID, "dims above " + std::to_string(max_dims) +
-                                       " need the distance-block workspace of hdb_plan_*; the no-allocation "
-                                       "entry point keeps no room for it");
+        return fail(HDB_E_INVALID,
+                    std::string("dims of ") + std::to_string(dims) + " exceed the no-allocation limit for " +
+                        (precision == HDB_F32 ? "float32" : "float64") + " windows of " + std::to_string(n) +
+                        " points (" + (max_dims ? "at most " + std::to_string(max_dims) + " dims" : "not supported") +
+                        "; larger windows or dims need the distance-block workspace of hdb_plan_*)");
 
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);

@@ -451,7 +451,7 @@ __device__ void linkage_warp(const Arena<Real>& a, int n) {
 // next_label (warp-uniform).
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
+__device__ int condense_warp(const Arena<Real>& a, int n, int mcs, int32_t* cl_size = nullptr) {
     using T = RealTraits<Real>;
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
@@ -474,7 +474,11 @@ __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
         dparent[right[i]] = (int16_t)(n + i);
     }
     const int root = 2 * n - 2;
-    if (lane == 0) { queue[0] = (int16_t)root; relabel[root - n] = (int16_t)n; }
+    if (lane == 0) {
+        queue[0] = (int16_t)root;
+        relabel[root - n] = (int16_t)n;
+        if (cl_size) cl_size[0] = n;
+    }
     __syncwarp();
     int head = 0, tail = 1, next_label = n + 1;
     while (head < tail) {  // tail <= n - 1 (every node is queued at most once)
@@ -515,6 +519,7 @@ __device__ int condense_warp(const Arena<Real>& a, int n, int mcs) {
                         parent[label - n] = (int16_t)cluster;
                         birth[label - n] = lambda;
                         a.sel[label - n] = 1;
+                        if (cl_size) cl_size[label - n] = csize;
                         st = T::add(st, T::mul(T::sub(lambda, cb), (Real)csize));
                         queue[pos + k] = (int16_t)child;
                     }

@@ -8,8 +8,9 @@ with NVRTC through CuPy (hdbscan_gpu/_cuda.py:18-42).  Their serial branch
 with g++ and runs here without CuPy or a GPU.
 
 This script reads the strings from the reference checkout where it lies
-(default /root/reference, or $HDB_REFERENCE), writes the generated translation
-units ONLY into oracle/_ref/ (git-ignored, never committed) and compiles
+($HDB_REFERENCE, a path given on the command line, or else a checkout named
+"reference" beside this repository), writes the generated translation units
+ONLY into oracle/_ref/ (git-ignored, never committed) and compiles
 oracle/_ref/libhdb_ref.so.  When the reference checkout is absent but the
 generated sources are present (a copy of this tree on another machine), it
 compiles those.  Uses: validating the oracle restatement, generating the
@@ -28,7 +29,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 LIBRARY = OUT / "libhdb_ref.so"
-DEFAULT_REFERENCE = Path(os.environ.get("HDB_REFERENCE", "/root/reference"))
+DEFAULT_REFERENCE = Path(os.environ["HDB_REFERENCE"]) if os.environ.get("HDB_REFERENCE") else \
+    HERE.parent.parent / "reference"
 
 
 def _load_kernels(reference: Path):

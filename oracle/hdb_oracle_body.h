@@ -560,6 +560,69 @@ int FN(hdb_oracle_batch)(const REAL* x, const int64_t* offsets, int windows, int
     return 0;
 }
 
+/* Ragged batch with every stage's state, over host threads (parity tests).
+ * `out` members point at packed arrays laid out as the GPU exports are: edge
+ * rows of window w at offsets[w] - w, point and cluster rows at offsets[w],
+ * n_clusters at w; NULL members are skipped. */
+typedef struct {
+    const REAL* x;
+    const int64_t* offsets;
+    int windows, d, mcs, ms;
+    double eps;
+    const FN(hdb_oracle_out)* out;
+    int32_t* status;
+    int next; /* shared ticket */
+} FN(hdb_batch_ex_job);
+
+#define HDB_AT(ptr, at) ((ptr) ? (ptr) + (at) : NULL)
+
+static void* FN(hdb_batch_ex_worker)(void* arg) {
+    FN(hdb_batch_ex_job)* job = (FN(hdb_batch_ex_job)*)arg;
+    const FN(hdb_oracle_out)* o = job->out;
+    for (;;) {
+        int w = __atomic_fetch_add(&job->next, 1, __ATOMIC_RELAXED);
+        if (w >= job->windows) break;
+        int64_t lo = job->offsets[w], hi = job->offsets[w + 1], e = lo - w;
+        FN(hdb_oracle_out) out;
+        out.labels = HDB_AT(o->labels, lo);
+        out.edges_uv = HDB_AT(o->edges_uv, 2 * e);
+        out.edge_w = HDB_AT(o->edge_w, e);
+        out.order = HDB_AT(o->order, e);
+        out.link_lr = HDB_AT(o->link_lr, 2 * e);
+        out.link_w = HDB_AT(o->link_w, e);
+        out.link_size = HDB_AT(o->link_size, e);
+        out.n_clusters = HDB_AT(o->n_clusters, w);
+        out.cl_parent = HDB_AT(o->cl_parent, lo);
+        out.cl_birth = HDB_AT(o->cl_birth, lo);
+        out.cl_stability = HDB_AT(o->cl_stability, lo);
+        out.cl_selected = HDB_AT(o->cl_selected, lo);
+        out.cl_size = HDB_AT(o->cl_size, lo);
+        out.point_parent = HDB_AT(o->point_parent, lo);
+        out.point_lambda = HDB_AT(o->point_lambda, lo);
+        out.core = HDB_AT(o->core, lo);
+        out.core_nbr = HDB_AT(o->core_nbr, lo);
+        out.probabilities = HDB_AT(o->probabilities, lo);
+        int s = FN(hdb_oracle_cluster)(job->x + lo * job->d, (int)(hi - lo), job->d, job->mcs, job->ms, job->eps,
+                                       &out);
+        if (job->status) job->status[w] = s;
+    }
+    return NULL;
+}
+
+#undef HDB_AT
+
+int FN(hdb_oracle_batch_ex)(const REAL* x, const int64_t* offsets, int windows, int d, int mcs, int ms,
+                            double eps, const FN(hdb_oracle_out)* out, int32_t* status, int threads) {
+    FN(hdb_batch_ex_job) job = {x, offsets, windows, d, mcs, ms, eps, out, status, 0};
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    pthread_t tid[256];
+    for (int t = 1; t < threads; ++t) pthread_create(&tid[t], NULL, FN(hdb_batch_ex_worker), &job);
+    FN(hdb_batch_ex_worker)(&job);
+    for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+    return 0;
+}
+
 #undef FN
 #undef HDB_CAT
 #undef HDB_CAT2

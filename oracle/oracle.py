@@ -61,6 +61,10 @@ def lib():
                 fn.restype = ctypes.c_int
                 fn.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                _P, _P, ctypes.c_int]
+                fn = getattr(handle, f"hdb_oracle_batch_ex_{suffix}")
+                fn.restype = ctypes.c_int
+                fn.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                               ctypes.POINTER(_Out), _P, ctypes.c_int]
                 fn = getattr(handle, f"hdb_oracle_distances_{suffix}")
                 fn.restype = None
                 fn.argtypes = [_P, ctypes.c_int, ctypes.c_int, _P]
@@ -214,3 +218,44 @@ def batch(packed, offsets, min_cluster_size, min_samples=None, epsilon=0.0, prec
         _ptr(labels), _ptr(status), int(threads),
     )
     return labels, status
+
+
+def batch_ex(packed, offsets, min_cluster_size, min_samples=None, epsilon=0.0, precision="float64", threads=None):
+    """Every stage's state for a ragged batch, packed as the GPU exports are:
+    edge rows of window w at offsets[w] - w, point and cluster rows at
+    offsets[w], n_clusters[w].  Windows run on host threads."""
+    dtype, suffix = _dtype(precision)
+    packed = np.ascontiguousarray(packed, dtype=dtype)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    windows = len(offsets) - 1
+    T = int(offsets[-1])
+    E = max(T - windows, 1)
+    ms = min_cluster_size if min_samples is None else min_samples
+    out = {
+        "labels": np.empty(T, np.int32),
+        "edges_uv": np.empty((E, 2), np.int32),
+        "edge_w": np.empty(E, dtype),
+        "order": np.empty(E, np.int32),
+        "link_lr": np.empty((E, 2), np.int32),
+        "link_w": np.empty(E, dtype),
+        "link_size": np.empty(E, np.int32),
+        "n_clusters": np.zeros(windows, np.int32),
+        "cl_parent": np.zeros(T, np.int32),
+        "cl_birth": np.zeros(T, dtype),
+        "cl_stability": np.zeros(T, dtype),
+        "cl_selected": np.zeros(T, np.uint8),
+        "cl_size": np.zeros(T, np.int32),
+        "point_parent": np.empty(T, np.int32),
+        "point_lambda": np.empty(T, dtype),
+        "core": np.empty(T, dtype),
+        "core_nbr": np.empty(T, np.int32),
+        "probabilities": np.empty(T, dtype),
+    }
+    struct = _Out(*[out[name].ctypes.data for name in _FIELDS])
+    status = np.zeros(windows, np.int32)
+    threads = threads or len(os.sched_getaffinity(0))
+    getattr(lib(), f"hdb_oracle_batch_ex_{suffix}")(
+        _ptr(packed), _ptr(offsets), windows, packed.shape[1], int(min_cluster_size), int(ms), float(epsilon),
+        ctypes.byref(struct), _ptr(status), int(threads))
+    out["status"] = status
+    return out

@@ -229,3 +229,44 @@ def test_cluster_rule_holds_one_wave(cuda):
         n_clustered = sum(c["windows"] for c in clustered)
         assert min(c["nmax"] for c in clustered) >= sizes[n_clustered - 1]  # the largest windows keep the cluster
         assert max(c["nmax"] for c in single) <= sizes[n_clustered]
+
+
+def test_cluster_waits_give_up_and_report_internal_status(cuda):
+    """A ticket that is never broadcast (test switch HDB_FLAG_TEST_STALL): every
+    CTA's bounded mbarrier wait runs out after 1 ms, the kernel ends with the
+    internal-error status and writes no labels, and the context stays usable.
+    Nothing is in flight when the waits give up (no record was sent)."""
+    import time
+
+    import torch
+
+    from hdbscan_gb300 import _lib
+    from hdbscan_gb300._cuda import Plan, pack, raise_for_status
+
+    rng = np.random.default_rng(17)
+    windows = [_mixture(rng, 1500, 8), _mixture(rng, 1300, 8), _mixture(rng, 1100, 8)]
+    packed, offsets = pack(windows, "float32")
+    with forced_variant("float32", 512, 2, 8, 2):
+        stalled = Plan(offsets, 8, min_cluster_size=5, min_samples=2, precision="float32",
+                       test_flags=_lib.HDB_FLAG_TEST_STALL)
+        normal = Plan(offsets, 8, min_cluster_size=5, min_samples=2, precision="float32")
+    assert all(c["cluster"] == 2 for c in json.loads(stalled.describe())["classes"])
+    labels = torch.full((stalled.points,), -7, dtype=torch.int32, device=cuda)
+    t0 = time.perf_counter()
+    _, status = stalled.forward(packed, labels=labels)
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    assert int(status.item()) == _lib.STATUS_INTERNAL
+    assert bool((labels == -7).all()), "a stalled kernel must not write labels"
+    assert elapsed < 5.0
+    with pytest.raises(RuntimeError, match="consistency"):
+        raise_for_status(int(status.item()))
+    # The same windows without the switch: the context still works and the
+    # labels equal the oracle's.
+    got, status = normal.forward(packed)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got = got.cpu().numpy()
+    for w, x in enumerate(windows):
+        want = oracle.cluster(np.asarray(x, np.float32), 5, 2, 0.0, "float32")["labels"]
+        np.testing.assert_array_equal(got[offsets[w]:offsets[w + 1]], want)

@@ -183,3 +183,45 @@ def test_default_selection_is_the_reference_contract():
     base = _run(case, "float64")
     ext = oracle.cluster(case["x"], 5, 5, 0.1, "float64", method="eom", allow_single_cluster=False)
     np.testing.assert_array_equal(base["labels"], ext["labels"])
+
+
+def test_batch_ex_packs_every_window_like_single_calls():
+    """oracle.batch_ex (threads over windows) equals per-window oracle.cluster, packed as the GPU exports."""
+    from hdbscan_gb300 import synthetic
+
+    packed, offsets, p = synthetic.make("c3", windows=6, high=700)
+    for precision in PRECISIONS:
+        batch = oracle.batch_ex(packed, offsets, p["min_cluster_size"], p["min_samples"],
+                                p["cluster_selection_epsilon"], precision, threads=3)
+        for w in range(len(offsets) - 1):
+            lo, hi = offsets[w], offsets[w + 1]
+            one = oracle.cluster(packed[lo:hi], p["min_cluster_size"], p["min_samples"],
+                                 p["cluster_selection_epsilon"], precision)
+            k = int(batch["n_clusters"][w])
+            assert k == len(one["cl_parent"])
+            for name in ("labels", "point_parent", "core"):
+                np.testing.assert_array_equal(_bits(batch[name][lo:hi]), _bits(one[name]))
+            np.testing.assert_array_equal(_bits(batch["point_lambda"][lo:hi]), _bits(one["point_lambda"]))
+            for name in ("edges_uv", "edge_w", "order", "link_lr", "link_w", "link_size"):
+                np.testing.assert_array_equal(_bits(batch[name][lo - w:hi - w - 1]), _bits(one[name]))
+            for name in ("cl_parent", "cl_birth", "cl_stability", "cl_selected", "cl_size"):
+                np.testing.assert_array_equal(_bits(batch[name][lo:lo + k]), _bits(one[name]))
+
+
+def test_condensed_tree_rows_equal_sklearn():
+    """hdbscan_gb300.condensed_tree on the oracle's exports gives scikit-learn's condensed_tree_ rows."""
+    torch = pytest.importorskip("torch")
+    from hdbscan_gb300 import condensed_tree
+
+    case = golden.load("configs")["c1"]
+    x = case["x"]
+    offsets = np.array([0, len(x)], np.int64)
+    mcs, ms, eps = case["params"]
+    out = oracle.batch_ex(x, offsets, int(mcs), int(ms), float(eps), "float64", threads=1)
+    hierarchy = {k: torch.from_numpy(v) for k, v in out.items() if isinstance(v, np.ndarray)}
+    tree = {k: v.numpy() for k, v in condensed_tree(hierarchy, offsets)[0].items()}
+    got = list(zip(tree["parent"].tolist(), tree["child"].tolist(), tree["lambda_val"].tolist(),
+                   tree["child_size"].tolist()))
+    want = sorted(zip(case["sk_ct_parent"].tolist(), case["sk_ct_child"].tolist(), case["sk_ct_lambda"].tolist(),
+                      case["sk_ct_size"].tolist()), key=lambda r: r[1])
+    assert got == want
