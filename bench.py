@@ -264,6 +264,7 @@ def run_reference_arm(args, packed, offsets, params):
             times.append(elapsed)
     per_step = statistics.median(times)
     value = count / per_step
+    reference_cuda = reference_cuda_timing(args, packed, offsets, params)
     line = {
         "impl": "reference", "metric": "windows_per_s", "value": value, "unit": "windows/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
@@ -272,8 +273,42 @@ def run_reference_arm(args, packed, offsets, params):
         "cpu_baseline": {"value": value, "unit": "windows/s", "cores": threads, "kind": kind,
                          "sample": f"first {count} windows of the workload per step"},
         "e2e": {"value": value, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_cuda": reference_cuda,
     }
     print(json.dumps(line))
+
+
+def reference_cuda_timing(args, packed, offsets, params, passes=3):
+    """The reference's own CUDA path on this GPU (oracle/ref_cuda.py: its kernel strings compiled
+    by NVRTC with --fmad=false, its host path of hdbscan_gpu/_cuda.py:91-128) over the whole
+    workload, device-resident input; ragged windows become dense calls grouped by size under its
+    512 MiB distance-buffer cap, as its API requires.  None without a GPU or kernel strings."""
+    try:
+        import torch
+
+        from oracle import ref_cuda
+    except Exception as error:
+        return {"unavailable": f"cannot import torch/oracle.ref_cuda: {error}"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA GPU on this host"}
+    if not ref_cuda.available():
+        return {"unavailable": "the reference's kernel strings were not generated (oracle/_ref/ref_cuda_source.json)"}
+    precision = params["precision"]
+    mcs, ms, eps = params["min_cluster_size"], params["min_samples"], params["cluster_selection_epsilon"]
+    X = torch.as_tensor(packed, dtype=torch.float32 if precision == "float32" else torch.float64, device="cuda")
+    ref_cuda.cluster_windows(X, offsets, mcs, ms, eps, precision)  # warm-up: NVRTC compiles
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(passes):
+        t0 = time.perf_counter()
+        ref_cuda.cluster_windows(X, offsets, mcs, ms, eps, precision)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    windows = len(offsets) - 1
+    per_pass = statistics.median(times)
+    return {"value": windows / per_pass, "unit": "windows/s", "ms_per_pass": per_pass * 1e3, "passes": passes,
+            "windows": windows, "note": "the reference's kernels and host path on this GPU, device-resident input, "
+                                        "dense calls grouped by window size under its 512 MiB cap"}
 
 
 def dist_env():

@@ -77,6 +77,20 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> bool:
         "REAL_WORKSPACE": kernels.REAL_WORKSPACE,
     }
     (OUT / "layout.json").write_text(json.dumps(layout, indent=1))
+    # The CUDA-C strings as the reference's NVRTC path assembles them
+    # (hdbscan_gpu/_cuda.py:18-42), for oracle/ref_cuda.py on a GPU.
+    cuda = {
+        "header": {p: kernels.header("cuda", p) for p in ("float32", "float64")},
+        "distance": kernels.DISTANCE_SOURCE,
+        "cluster": kernels.CLUSTER_SOURCE,
+        "cluster_threads": kernels.CLUSTER_THREADS,
+        "integer_workspace": kernels.INTEGER_WORKSPACE,
+        "real_workspace": kernels.REAL_WORKSPACE,
+    }
+    target = OUT / "ref_cuda_source.json"
+    text = json.dumps(cuda)
+    if not target.exists() or target.read_text() != text:
+        target.write_text(text)
     return True
 
 
