@@ -271,6 +271,10 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
     const int hi = min(n, lo + chunk);
 
     // ---- slots and validation ------------------------------------------------
+    // Slot layout as in hdb_forward.cuh: lane-major for the matrix variant
+    // (coalesced row reads), thread-major for the register variants.
+    constexpr bool kLaneMajor = DP == 0;
+    auto slot_of = [&](int v) { return kLaneMajor ? warp * 32 * SV + v * 32 + lane : tid * SV + v; };
     Real xr[SV][DPS];
     Real best[SV], thr[SV], core_r[SV];
     int src[SV], vid[SV];
@@ -285,8 +289,8 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
     };
 #pragma unroll
     for (int v = 0; v < SV; ++v) {
-        const int j = lo + tid * SV + v;
-        const bool valid = tid * SV + v < L && j < hi;
+        const int j = lo + slot_of(v);
+        const bool valid = slot_of(v) < L && j < hi;
         vid[v] = valid ? j : -1;
         act[v] = valid && j != 0;  // vertex 0 starts the tree (_kernels.py:210-213)
         best[v] = T::inf();
@@ -328,26 +332,47 @@ __device__ __forceinline__ int cluster_window(const ForwardArgs& args, const Clu
         for (int it = 0; it < n - 1; ++it) {
             if (it > 0 && (it & 31) == 0) {
                 // ---- compaction checkpoint (CTA-uniform decision) -------------
+                // Live vertices are staged in slot order and re-packed into
+                // slots [0, live).
+                unsigned bal[SV];
                 int count = 0;
 #pragma unroll
-                for (int v = 0; v < SV; ++v) count += act[v] ? 1 : 0;
+                for (int v = 0; v < SV; ++v) {
+                    bal[v] = __ballot_sync(0xffffffffu, act[v]);
+                    count += kLaneMajor ? __popc(bal[v]) : (act[v] ? 1 : 0);
+                }
                 int total = 0;
-                int pos = active_exclusive_scan(count, aw, s_scan, total);
+                int pos = active_exclusive_scan(kLaneMajor ? (lane == 0 ? count : 0) : count, aw, s_scan, total);
                 if (live - total >= 32 * SV) {
+                    if constexpr (kLaneMajor) {
+                        pos = __shfl_sync(0xffffffffu, pos, 0);  // slots of the warps before this one
+                        const unsigned below = lanemask_lt();
 #pragma unroll
-                    for (int v = 0; v < SV; ++v) {
-                        if (act[v]) {
-                            stage_j[pos] = (int16_t)vid[v];
-                            stage_src[pos] = (int16_t)src[v];
-                            stage_best[pos] = best[v];
-                            ++pos;
+                        for (int v = 0; v < SV; ++v) {
+                            if (act[v]) {
+                                const int at = pos + __popc(bal[v] & below);
+                                stage_j[at] = (int16_t)vid[v];
+                                stage_src[at] = (int16_t)src[v];
+                                stage_best[at] = best[v];
+                            }
+                            pos += __popc(bal[v]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < SV; ++v) {
+                            if (act[v]) {
+                                stage_j[pos] = (int16_t)vid[v];
+                                stage_src[pos] = (int16_t)src[v];
+                                stage_best[pos] = best[v];
+                                ++pos;
+                            }
                         }
                     }
                     bar_sync(kBarIter, aw * 32);
                     live = total;
 #pragma unroll
                     for (int v = 0; v < SV; ++v) {
-                        const int slot = tid * SV + v;
+                        const int slot = slot_of(v);
                         if (slot < live) {
                             vid[v] = stage_j[slot];
                             src[v] = stage_src[slot];

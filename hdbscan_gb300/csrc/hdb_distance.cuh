@@ -147,8 +147,25 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
                         }
                 }
             };
-            if (int_square) accumulate([](Real d) { return T::sqr(d); });
-            else accumulate([](Real d) { return T::mul(d, d); });
+            if (int_square) {
+                // Squares on the integer pipes (hdb_exact.h); half of the
+                // running sums (pairs with a + b odd) add on the integer pipes
+                // too, the other half on the FP64 pipe, which balances them.
+                for (int k = 0; k < kend; ++k) {
+                    Real xi[4], xj[4];
+                    DistVec<Real>::load4(&s_i[k][ty * 4], xi);
+                    DistVec<Real>::load4(&s_j[k][tx * 4], xj);
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const Real sq = T::sqr(T::sub(xi[a], xj[b]));
+                            acc[a][b] = ((a + b) & 1) ? add_rn_nonneg(acc[a][b], sq) : T::add(acc[a][b], sq);
+                        }
+                }
+            } else {
+                accumulate([](Real d) { return T::mul(d, d); });
+            }
         }
         __syncthreads();
     }
@@ -541,6 +558,129 @@ __global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_key_kernel(co
         if (t == args.ms - 1) { value = L[t]; index = LI[t]; }
     static_cast<double*>(args.core)[base + i] = T::from_key(value);
     if (args.core_nbr) args.core_nbr[base + i] = index;
+}
+
+// Rows of the materialized matrix, one warp per row, for lists of K <= 32
+// (both precisions).  The warp reads 32 consecutive entries of its row per
+// load (coalesced), keeps the K smallest (key, index) pairs one per lane
+// (lane t holds position t, ascending), and filters every entry with one
+// integer compare against the current K-th key; entries below it are
+// inserted one at a time in index order by the whole warp (shift by one
+// shuffle), so the list is exactly the one the serial strict-'<' scan in
+// index order builds: the K smallest in (value, index) order.  The first 32
+// entries are placed by a warp bitonic sort on (key, index).  Keys are the
+// order-preserving bit patterns of the non-negative distances (integer
+// compares only; float64 keys compare as 32-bit word pairs).  Replaces the
+// thread-per-row scans, whose insertions diverged within the warp.
+constexpr int kCoreRowsWarps = 8;  // warps per CTA; an item's 32 rows are shared among them
+
+template <typename Key>
+__device__ __forceinline__ Key shfl_key(Key k, int src) {
+    if constexpr (sizeof(Key) == 4) {
+        return __shfl_sync(0xffffffffu, k, src);
+    } else {
+        const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(k >> 32), src);
+        const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)k, src);
+        return ((Key)hi << 32) | lo;
+    }
+}
+template <typename Key>
+__device__ __forceinline__ Key shfl_key_up(Key k) {
+    if constexpr (sizeof(Key) == 4) {
+        return __shfl_up_sync(0xffffffffu, k, 1);
+    } else {
+        const uint32_t hi = __shfl_up_sync(0xffffffffu, (uint32_t)(k >> 32), 1);
+        const uint32_t lo = __shfl_up_sync(0xffffffffu, (uint32_t)k, 1);
+        return ((Key)hi << 32) | lo;
+    }
+}
+template <typename Key>
+__device__ __forceinline__ Key shfl_key_xor(Key k, int mask) {
+    if constexpr (sizeof(Key) == 4) {
+        return __shfl_xor_sync(0xffffffffu, k, mask);
+    } else {
+        const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(k >> 32), mask);
+        const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)k, mask);
+        return ((Key)hi << 32) | lo;
+    }
+}
+template <typename Key>
+__device__ __forceinline__ Key key_select(bool c, Key a, Key b) {
+    if constexpr (sizeof(Key) == 4) {
+        return c ? a : b;
+    } else {
+        return core_key_sel(c, a, b);
+    }
+}
+
+template <typename Real, int K>
+__global__ void __launch_bounds__(32 * kCoreRowsWarps) hdb_core_rows_kernel(const CoreArgs args) {
+    static_assert(K <= 32, "one list entry per lane");
+    using T = RealTraits<Real>;
+    using Key = typename T::Bits;
+    constexpr Key kNone = (Key)~(Key)0;  // above every distance key (and +inf's)
+    constexpr int U = 8;                 // row loads in flight per lane
+    const int item = blockIdx.x;
+    if (item >= args.n_items) return;
+    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
+    const int64_t base = args.offsets[w];
+    const int n = (int)(args.offsets[w + 1] - base);
+    const Real* __restrict__ Dw = static_cast<const Real*>(args.dist) + args.dist_offsets[w];
+    const int64_t ld = dist_ld(n);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < kCoreMatrixRows; r += kCoreRowsWarps) {
+        const int i = r0 + r;
+        if (i >= n) break;  // warp-uniform
+        const Real* __restrict__ row = Dw + (int64_t)i * ld;
+        // First 32 entries: bitonic sort on (key, index), ascending.
+        Key lk = lane < n ? T::key(__ldcs(row + lane)) : kNone;
+        int li = lane;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const Key pk = shfl_key_xor(lk, j);
+                const int pi = __shfl_xor_sync(0xffffffffu, li, j);
+                const bool partner_less = key_lt(pk, lk) || (key_eq(pk, lk) && pi < li);
+                const bool keep_min = ((lane & k) == 0) == ((lane & j) == 0);
+                const bool take = keep_min ? partner_less : !partner_less;
+                lk = key_select(take, pk, lk);
+                li = take ? pi : li;
+            }
+        }
+        Key tau = shfl_key(lk, K - 1);
+        for (int j0 = 32; j0 < n; j0 += 32 * U) {
+            Key v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int j = j0 + 32 * u + lane;
+                v[u] = j < n ? T::key(__ldcs(row + j)) : kNone;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                unsigned bal = __ballot_sync(0xffffffffu, key_lt(v[u], tau));
+                while (bal) {
+                    const int src = __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    const Key ck = shfl_key(v[u], src);
+                    if (key_lt(ck, tau)) {  // warp-uniform; tau only decreases
+                        const int cj = j0 + 32 * u + src;
+                        const Key pk = shfl_key_up(lk);
+                        const int pi = __shfl_up_sync(0xffffffffu, li, 1);
+                        const bool shift = lane > 0 && key_lt(ck, pk);
+                        const bool place = !shift && key_lt(ck, lk);
+                        lk = key_select(shift, pk, key_select(place, ck, lk));
+                        li = shift ? pi : (place ? cj : li);
+                        tau = shfl_key(lk, K - 1);
+                    }
+                }
+            }
+        }
+        if (lane == args.ms - 1) {
+            static_cast<Real*>(args.core)[base + i] = T::from_key(lk);
+            if (args.core_nbr) args.core_nbr[base + i] = li;
+        }
+    }
 }
 
 // Any ms: one CTA (256 threads) per row; the row is computed (or read) into

@@ -1,11 +1,14 @@
-// Exact IEEE-754 binary64 squaring on the integer pipes.
+// Exact IEEE-754 binary64 squaring and non-negative addition on the integer
+// pipes.
 //
 // GB300's FP64 pipe is a small fraction of its FP32/INT32 throughput, and the
 // float64 distance kernel (three FP64 operations per coordinate: subtract,
 // square, add) runs at that pipe's limit.  sqr_rn(d) returns the correctly
 // rounded (round-to-nearest-even) square of d computed with 32x32->64-bit
-// integer products, so the square moves to the integer pipes and only the
-// subtraction and the addition stay on the FP64 pipe.  The result is
+// integer products, so the square moves to the integer pipes; add_rn_nonneg
+// (end of this file) does the same for the running sum, which the distance
+// kernel applies to half of its accumulators so that the FP64 pipe and the
+// integer pipes carry balanced loads.  The square's result is
 // bit-identical to d*d under IEEE-754 for every input: zero returns +0, and
 // values whose square is not a normal double (|d| < 2^-511 or |d| >= 2^511,
 // subnormals, infinities, NaN) take the hardware multiply behind a
@@ -184,6 +187,86 @@ HDB_HD double sqr_rn(double d) {
     if (hw) r = d * d;
 #endif
     return r;
+}
+
+// Correctly rounded a + b of two non-negative doubles (zero, subnormal,
+// normal or +inf; no NaN, sign bits clear), on 32-bit words only: the float64
+// distance accumulator's addition moved off the FP64 pipe.  Method (the
+// textbook same-sign addition): the larger operand's significand and the
+// smaller one's (hidden bit for normals, effective exponent 1 for
+// subnormals), both extended by 3 guard bits, are aligned by the exponent
+// difference with every shifted-out bit OR-ed into the lowest (sticky) bit;
+// the sum has at most one carry bit, removed by a sticky shift; the top 53
+// bits are rounded to nearest-even on the guard and sticky bits; the biased
+// exponent minus one plus the significand (hidden bit included) packs the
+// result, so a rounding carry or a subnormal sum reaching 2^52 moves into the
+// exponent field, and an exponent of 2047 becomes +inf.
+HDB_HD void add_rn_nonneg_words(uint32_t ahi, uint32_t alo, uint32_t bhi, uint32_t blo, uint32_t& rhi,
+                                uint32_t& rlo) {
+    const bool a_big = ahi > bhi || (ahi == bhi && alo >= blo);
+    const uint32_t xhi = a_big ? ahi : bhi, xlo = a_big ? alo : blo;  // larger
+    const uint32_t yhi = a_big ? bhi : ahi, ylo = a_big ? blo : alo;  // smaller
+    const uint32_t fx = xhi >> 20, fy = yhi >> 20;  // exponent fields (sign bits clear)
+    const uint32_t ex = fx ? fx : 1u, ey = fy ? fy : 1u;
+    const uint32_t d = ex - ey;
+    // Significands (hidden bit for normals), shifted left by 3: 56 bits in (hi:24, lo:32).
+    const uint32_t xh = (((xhi & 0xfffffu) | (fx ? 0x100000u : 0u)) << 3) | (xlo >> 29), xl = xlo << 3;
+    const uint32_t yh = (((yhi & 0xfffffu) | (fy ? 0x100000u : 0u)) << 3) | (ylo >> 29), yl = ylo << 3;
+    // y >> d with sticky, d in [0, 56]; beyond that y only sets the sticky bit.
+    uint32_t ah, al, lost;
+    if (d < 32u) {
+        al = funnel_right(yl, yh, d);
+        ah = yh >> d;
+        lost = d ? (yl << (32u - d)) : 0u;
+    } else if (d < 57u) {
+        const uint32_t s = d - 32u;
+        al = yh >> s;
+        ah = 0u;
+        lost = yl | (s ? (yh << (32u - s)) : 0u);
+    } else {
+        al = 0u;
+        ah = 0u;
+        lost = 1u;
+    }
+    al |= lost != 0u ? 1u : 0u;
+    uint32_t c;
+    uint32_t sl = add_carry(xl, al, 0u, c);
+    uint32_t sh = xh + ah + c;
+    uint32_t e = ex;
+    if (sh >> 24) {  // carry out of the 56 bits: one sticky shift
+        sl = funnel_right(sl, sh, 1u) | (sl & 1u);
+        sh >>= 1;
+        e += 1u;
+    }
+    uint32_t ml = funnel_right(sl, sh, 3u);
+    uint32_t mh = sh >> 3;  // 21 bits, hidden bit at 20
+    const uint32_t guard = (sl >> 2) & 1u, sticky = sl & 3u;
+    const uint32_t up = guard & ((sticky != 0u ? 1u : 0u) | (ml & 1u));
+    ml = add_carry(ml, up, 0u, c);
+    mh += c;
+    uint32_t hi = ((e - 1u) << 20) + mh;
+    uint32_t lo = ml;
+    if (hi >= 0x7ff00000u || fx == 0x7ffu) { hi = 0x7ff00000u; lo = 0u; }  // overflow or an infinite operand
+    const bool y_zero = (yhi | ylo) == 0u;
+    rhi = y_zero ? xhi : hi;
+    rlo = y_zero ? xlo : lo;
+}
+
+HDB_HD double add_rn_nonneg(double a, double b) {
+#ifdef __CUDA_ARCH__
+    const uint32_t ahi = (uint32_t)__double2hiint(a), alo = (uint32_t)__double2loint(a);
+    const uint32_t bhi = (uint32_t)__double2hiint(b), blo = (uint32_t)__double2loint(b);
+#else
+    const uint64_t ab = exact_bits(a), bb = exact_bits(b);
+    const uint32_t ahi = (uint32_t)(ab >> 32), alo = (uint32_t)ab, bhi = (uint32_t)(bb >> 32), blo = (uint32_t)bb;
+#endif
+    uint32_t rhi, rlo;
+    add_rn_nonneg_words(ahi, alo, bhi, blo, rhi, rlo);
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)rhi, (int)rlo);
+#else
+    return exact_double(((uint64_t)rhi << 32) | rlo);
+#endif
 }
 
 }  // namespace hdb

@@ -15,7 +15,8 @@
 // roles simply alternate.
 //
 // Prim details:
-//  * slot s lives in thread s / SV (vertex id vid); the thread keeps the
+//  * slot s lives in thread s / SV (vertex id vid; the matrix variant lays
+//    slots out lane-major so that row reads coalesce); the thread keeps the
 //    vertex's coordinates (zero-padded to DP, exact) in registers, its best
 //    weight, source and an in-tree bit;
 //  * the current vertex's coordinates come from the window staged in shared
@@ -139,12 +140,19 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int D = args.D;
 
-    // Per-slot state.  Slot s = tid*SV + v; xr holds the coordinates, act marks
-    // slots holding a vertex outside the tree.  Float distances use packed
+    // Per-slot state.  Register variants: slot s = tid*SV + v.  Matrix variant:
+    // slot s = warp*32*SV + v*32 + lane (lane-major), so that for each v the
+    // warp's 32 row reads fall on consecutive slots, whose vertex ids increase
+    // (one 128-byte line before any vertex left the tree) instead of one float
+    // per 32-byte sector SV times over.  Either way warp w owns slots
+    // [w*32*SV, (w+1)*32*SV).  xr holds the coordinates, act marks slots
+    // holding a vertex outside the tree.  Float distances use packed
     // f32x2 instructions for the differences and squares only; the sum stays a
     // chain of scalar round-to-nearest adds in k order (a packed multiply
     // feeding a packed add may be contracted into a packed FMA, which would
     // change the rounding).
+    constexpr bool kLaneMajor = DP == 0;
+    auto slot_of = [&](int v) { return kLaneMajor ? warp * 32 * SV + v * 32 + lane : tid * SV + v; };
     Real xr[SV][DPS];
     Real best[SV], thr[SV], core_r[SV];
     int src[SV], vid[SV];
@@ -155,7 +163,7 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
     };
 #pragma unroll
     for (int v = 0; v < SV; ++v) {
-        const int j = tid * SV + v;
+        const int j = slot_of(v);
         vid[v] = j < n ? j : -1;
         act[v] = j < n && j != 0;  // vertex 0 starts the tree (_kernels.py:210-213)
         best[v] = T::inf();
@@ -179,28 +187,50 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
         const int remaining = n - 1 - it;  // vertices still outside the tree
         if (live - remaining >= kCompactAfter) {
             // ---- compaction over the active warps ----------------------------
-            int count = 0;
-#pragma unroll
-            for (int v = 0; v < SV; ++v) count += act[v] ? 1 : 0;
-            int total = 0;
-            int pos = active_exclusive_scan(count, aw, s_scan, total);
+            // Live vertices are staged in slot order (so slots keep increasing
+            // vertex ids) and re-packed into slots [0, live).
             int16_t* stage_j = arena.s2;
             int16_t* stage_src = arena.s3;
             Real* stage_best = arena.r1;
+            int total = 0;
+            if constexpr (kLaneMajor) {
+                unsigned bal[SV];
+                int wcount = 0;
 #pragma unroll
-            for (int v = 0; v < SV; ++v) {
-                if (act[v]) {
-                    stage_j[pos] = (int16_t)vid[v];
-                    stage_src[pos] = (int16_t)src[v];
-                    stage_best[pos] = best[v];
-                    ++pos;
+                for (int v = 0; v < SV; ++v) { bal[v] = __ballot_sync(0xffffffffu, act[v]); wcount += __popc(bal[v]); }
+                int pos = active_exclusive_scan(lane == 0 ? wcount : 0, aw, s_scan, total);
+                pos = __shfl_sync(0xffffffffu, pos, 0);  // slots of the warps before this one
+                const unsigned below = lanemask_lt();
+#pragma unroll
+                for (int v = 0; v < SV; ++v) {
+                    if (act[v]) {
+                        const int at = pos + __popc(bal[v] & below);
+                        stage_j[at] = (int16_t)vid[v];
+                        stage_src[at] = (int16_t)src[v];
+                        stage_best[at] = best[v];
+                    }
+                    pos += __popc(bal[v]);
+                }
+            } else {
+                int count = 0;
+#pragma unroll
+                for (int v = 0; v < SV; ++v) count += act[v] ? 1 : 0;
+                int pos = active_exclusive_scan(count, aw, s_scan, total);
+#pragma unroll
+                for (int v = 0; v < SV; ++v) {
+                    if (act[v]) {
+                        stage_j[pos] = (int16_t)vid[v];
+                        stage_src[pos] = (int16_t)src[v];
+                        stage_best[pos] = best[v];
+                        ++pos;
+                    }
                 }
             }
             bar_sync(kBarIter, aw * 32);
             live = total;
 #pragma unroll
             for (int v = 0; v < SV; ++v) {
-                const int slot = tid * SV + v;
+                const int slot = slot_of(v);
                 if (slot < live) {
                     vid[v] = stage_j[slot];
                     src[v] = stage_src[slot];

@@ -37,10 +37,13 @@ cudaError_t launch_core_points(const CoreArgs& a, int grid, cudaStream_t s, int 
 
 template <typename Real, int K>
 cudaError_t launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
-    if constexpr (sizeof(Real) == 8 && K > 8)  // integer-key lists, one warp per 32 rows
+    if constexpr (K <= 32)  // one warp per row, list across the lanes
+        return launch_ex(hdb_core_rows_kernel<Real, K>, grid, 32 * kCoreRowsWarps, 0, s, priority, 1, a);
+    else if constexpr (sizeof(Real) == 8)  // integer-key lists, one warp per 32 rows
         return launch_ex(hdb_core_matrix_key_kernel<K>, grid, kCoreMatrixRows, 0, s, priority, 1, a);
-    return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows * core_segments<Real, K>(), 0, s,
-                     priority, 1, a);
+    else
+        return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows * core_segments<Real, K>(), 0, s,
+                         priority, 1, a);
 }
 
 template <typename Real, int K, int DP>
@@ -50,9 +53,12 @@ constexpr CoreVariant core_points_variant() {
 
 template <typename Real, int K>
 constexpr CoreVariant core_matrix_variant() {
-    if constexpr (sizeof(Real) == 8 && K > 8)
+    if constexpr (K <= 32)
+        return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_rows_kernel<Real, K>, launch_core_matrix<Real, K>};
+    else if constexpr (sizeof(Real) == 8)
         return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_key_kernel<K>, launch_core_matrix<Real, K>};
-    return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_kernel<Real, K>, launch_core_matrix<Real, K>};
+    else
+        return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_kernel<Real, K>, launch_core_matrix<Real, K>};
 }
 
 template <typename Real>
