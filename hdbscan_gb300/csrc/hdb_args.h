@@ -84,6 +84,8 @@ struct CoreArgs {
     int32_t* status;
 };
 
+constexpr int kBackwardWarps = 8;  // backward kernel: warps (32 linkage rows each) per CTA
+
 struct BackwardArgs {
     const void* X;               // [T, D]
     const int64_t* offsets;      // [B+1]

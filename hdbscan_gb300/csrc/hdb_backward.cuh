@@ -30,39 +30,64 @@ __device__ __forceinline__ Real exact_distance(const Real* xa, const Real* xb, i
     return T::sqrt_rn(acc);
 }
 
-// One thread per linkage row.
+// Each warp takes 32 consecutive linkage rows.  First every lane decides the
+// pair of its own row: the chosen pair's distance is the merge weight itself
+// (the distance term, or the core distance, which is the distance to the core
+// neighbour computed with the same arithmetic), so the exact distance d_uv is
+// recomputed only when a core distance ties the weight and the
+// distance-first rule needs to know whether d_uv ties it too.  Then the warp
+// scatters the rows one after another with the lanes over the coordinates:
+// the terms g (x_a - x_b) / w are independent per coordinate, so the loads of
+// x_a and x_b and the atomics on dX are coalesced.
 template <typename Real>
-__global__ void __launch_bounds__(256) hdb_backward_kernel(const BackwardArgs args) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= args.n_edges) return;
-    const int w = args.edge_window[r];
-    const int64_t base = args.offsets[w];
-    const int64_t ebase = base - w;
+__global__ void __launch_bounds__(32 * kBackwardWarps) hdb_backward_kernel(const BackwardArgs args) {
+    const int lane = threadIdx.x & 31;
+    const int first = (blockIdx.x * kBackwardWarps + (threadIdx.x >> 5)) * 32;
+    if (first >= args.n_edges) return;  // warp-uniform
+    const int r = first + lane;
     const int D = args.D;
     const Real* X = static_cast<const Real*>(args.X);
-    const Real g = static_cast<const Real*>(args.grad)[r];
-    if (g == Real(0)) return;
-    const Real wgt = static_cast<const Real*>(args.link_w)[r];
-    const int e = args.order[r];
-    const int u = args.edges_uv[2 * (ebase + e)], v = args.edges_uv[2 * (ebase + e) + 1];
-    int a = u, b = v;
-    const Real duv = exact_distance<Real>(X + (base + u) * D, X + (base + v) * D, D);
-    if (!args.unit_core && !(duv == wgt)) {
-        const Real* core = static_cast<const Real*>(args.core);
-        if (core[base + u] == wgt) { a = u; b = args.core_nbr[base + u]; }
-        else if (core[base + v] == wgt) { a = v; b = args.core_nbr[base + v]; }
+    int64_t row_a = -1, row_b = -1;  // global point rows of the pair, -1 = no gradient
+    Real scale = Real(0);
+    if (r < args.n_edges) {
+        const Real g = static_cast<const Real*>(args.grad)[r];
+        const Real wgt = static_cast<const Real*>(args.link_w)[r];
+        if (g != Real(0) && wgt > Real(0)) {
+            const int w = args.edge_window[r];
+            const int64_t base = args.offsets[w];
+            const int64_t ebase = base - w;
+            const int e = args.order[r];
+            const int u = args.edges_uv[2 * (ebase + e)], v = args.edges_uv[2 * (ebase + e) + 1];
+            int a = u, b = v;
+            if (!args.unit_core) {
+                const Real* core = static_cast<const Real*>(args.core);
+                const Real cu = core[base + u], cv = core[base + v];
+                if ((cu == wgt || cv == wgt) &&
+                    !(exact_distance<Real>(X + (base + u) * D, X + (base + v) * D, D) == wgt)) {
+                    if (cu == wgt) { a = u; b = args.core_nbr[base + u]; }
+                    else { a = v; b = args.core_nbr[base + v]; }
+                }
+            }
+            if (b >= 0 && a != b) {
+                row_a = base + a;
+                row_b = base + b;
+                scale = g / wgt;
+            }
+        }
     }
-    if (b < 0 || a == b) return;
-    const Real* xa = X + (base + a) * D;
-    const Real* xb = X + (base + b) * D;
-    const Real d = (a == u && b == v) ? duv : exact_distance<Real>(xa, xb, D);
-    if (!(d > Real(0))) return;
-    const Real scale = g / d;
     Real* dX = static_cast<Real*>(args.dX);
-    for (int k = 0; k < D; ++k) {
-        const Real c = scale * (xa[k] - xb[k]);
-        atomicAdd(dX + (base + a) * D + k, c);
-        atomicAdd(dX + (base + b) * D + k, -c);
+    for (int t = 0; t < 32; ++t) {
+        const int64_t ra = __shfl_sync(0xffffffffu, row_a, t);
+        if (ra < 0) continue;  // warp-uniform
+        const int64_t rb = __shfl_sync(0xffffffffu, row_b, t);
+        const Real sc = __shfl_sync(0xffffffffu, scale, t);
+        const Real* xa = X + ra * D;
+        const Real* xb = X + rb * D;
+        for (int k = lane; k < D; k += 32) {
+            const Real c = sc * (xa[k] - xb[k]);
+            atomicAdd(dX + ra * D + k, c);
+            atomicAdd(dX + rb * D + k, -c);
+        }
     }
 }
 

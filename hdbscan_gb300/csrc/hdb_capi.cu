@@ -1025,7 +1025,8 @@ int hdb_plan_backward(hdb_plan_t* p, const void* X, const hdb_exports_t* ex, con
     a.core = ex->core;
     a.core_nbr = ex->core_nbr;
     a.dX = dX;
-    if (a.n_edges > 0) HDB_CUDA(p->k->launch_backward(a, (a.n_edges + 255) / 256, s, 0));
+    if (a.n_edges > 0)
+        HDB_CUDA(p->k->launch_backward(a, (a.n_edges + 32 * hdb::kBackwardWarps - 1) / (32 * hdb::kBackwardWarps), s, 0));
     return HDB_OK;
 }
 

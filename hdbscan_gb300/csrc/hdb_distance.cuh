@@ -10,15 +10,14 @@
 //   Block row stride ld = round_up(n, 4) keeps every row 16-byte aligned.
 // * hdb_distance128_kernel: the same blocks for float32 windows of 384 points
 //   and more, 128x128 tiles with 8x8 pairs per thread (same arithmetic).
-// * hdb_core_points_kernel / hdb_core_matrix_kernel: core_i = the (ms-1)-th
+// * hdb_core_points_kernel / hdb_core_rows_kernel: core_i = the (ms-1)-th
 //   smallest distance of row i, self (0) included (reference:
-//   hdbscan_gpu/_cuda.py:114-118, cp.partition).  One thread per row keeps a
-//   sorted register list of the KMAX smallest (value, index) pairs; the value
-//   at position ms-1 is the order statistic, the index is the ms-th nearest
-//   neighbour in (distance, index) order (used by the backward pass).  The
-//   matrix kernel splits each row scan over column ranges (one warp each);
-//   hdb_core_matrix_key_kernel serves float64 lists longer than 8 with
-//   integer order keys.
+//   hdbscan_gpu/_cuda.py:114-118, cp.partition), from a list of the K
+//   smallest (value, index) pairs; the value at position ms-1 is the order
+//   statistic, the index is the ms-th nearest neighbour in (distance, index)
+//   order (used by the backward pass).  The points kernel recomputes the
+//   distances (one thread per row, a sorted register list); the rows kernel
+//   reads the materialized block (one warp per row, the list across lanes).
 // * hdb_core_select_kernel: any ms, one CTA per row, radix select on the
 //   order-preserving bit pattern of the non-negative distances.
 #pragma once
@@ -324,23 +323,8 @@ __global__ void __launch_bounds__(256, 2) hdb_distance128_kernel(const DistanceA
 // ---------------------------------------------------------------------------
 
 constexpr int kCoreRows = 128;        // rows per CTA of the points kernel
-constexpr int kCoreMatrixRows = 32;   // rows per CTA of the matrix kernel (one warp per row segment)
-constexpr int kCorePrefetch = 16;
-constexpr int kCoreSpanMin = 256;
+constexpr int kCoreMatrixRows = 32;   // rows per work item of the matrix (rows) kernel
 
-// Segments each row scan of the matrix kernel is split into (one warp each):
-// more loads in flight per SM; the partial lists fit 32 KB of shared memory.
-// Every segment fills its own list and a warp runs an insertion whenever one
-// of its 32 rows inserts, so float64 lists (costlier insertions) split only
-// when K = 8.
-template <typename Real, int K>
-__host__ __device__ constexpr int core_segments() {
-    constexpr int s = sizeof(Real) == 4 ? 128 / K : (K <= 8 ? 8 : 1);
-    return s < 1 ? 1 : (s > 8 ? 8 : s);
-}
-
-// Insert (d, j) into the ascending register list L/LI of length K; strict '<'
-// keeps earlier (smaller) indices ahead among equal values.
 template <typename Real, int K>
 __device__ __forceinline__ void topk_insert(Real (&L)[K], int (&LI)[K], Real d, int j) {
     using T = RealTraits<Real>;
@@ -431,147 +415,25 @@ __global__ void __launch_bounds__(kCoreRows) hdb_core_points_kernel(const CoreAr
     if (__syncthreads_or(overflow) && threadIdx.x == 0) atomic_status(args.status, kOverflow);
 }
 
-// Rows from the materialized matrix: thread i reads column i (the block is
-// symmetric), so every step is one coalesced row segment.  Warp s of the CTA
-// scans the s-th of S column ranges for the CTA's 32 rows; warp 0 then merges
-// the other warps' sorted lists in range order, which keeps (value, index)
-// order: equal values from lower ranges were inserted first.
-template <typename Real, int K>
-__global__ void __launch_bounds__(kCoreMatrixRows * core_segments<Real, K>())
-    hdb_core_matrix_kernel(const CoreArgs args) {
-    using T = RealTraits<Real>;
-    constexpr int S = core_segments<Real, K>();
-    __shared__ Real s_val[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
-    __shared__ int s_ix[S > 1 ? S - 1 : 1][K][kCoreMatrixRows];
-    const int item = blockIdx.x;
-    if (item >= args.n_items) return;
-    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
-    const int64_t base = args.offsets[w];
-    const int n = (int)(args.offsets[w + 1] - base);
-    const Real* __restrict__ Dw = static_cast<const Real*>(args.dist) + args.dist_offsets[w];
-    const int64_t ld = dist_ld(n);
-    const int r = threadIdx.x & (kCoreMatrixRows - 1), seg = threadIdx.x / kCoreMatrixRows;
-    const int i = r0 + r;
-    const bool row = i < n;
-    // At least kCoreSpanMin columns per range: small windows use fewer warps.
-    const int ranges = max(1, min(S, n / kCoreSpanMin));
-    const int span = ((n + ranges - 1) / ranges + kCorePrefetch - 1) / kCorePrefetch * kCorePrefetch;
-    const int jlo = min(n, seg * span), jhi = min(n, jlo + span);
-    Real L[K];
-    int LI[K];
-#pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::inf(); LI[t] = -1; }
-    if (row) {
-        // kCorePrefetch independent row loads in flight per thread.
-        int j0 = jlo;
-        for (; j0 + kCorePrefetch <= jhi; j0 += kCorePrefetch) {
-            Real v[kCorePrefetch];
-#pragma unroll
-            for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
-#pragma unroll
-            for (int u = 0; u < kCorePrefetch; ++u) topk_insert<Real, K>(L, LI, v[u], j0 + u);
-        }
-        for (int j = j0; j < jhi; ++j) topk_insert<Real, K>(L, LI, __ldcs(Dw + (int64_t)j * ld + i), j);
-    }
-    if constexpr (S > 1) {
-        if (seg > 0) {
-#pragma unroll
-            for (int t = 0; t < K; ++t) { s_val[seg - 1][t][r] = L[t]; s_ix[seg - 1][t][r] = LI[t]; }
-        }
-        __syncthreads();
-        if (seg == 0 && row) {
-            for (int q = 0; q < ranges - 1; ++q) {
-                for (int t = 0; t < K; ++t) {
-                    const Real d = s_val[q][t][r];
-                    if (!T::lt(d, L[K - 1])) break;  // the list is ascending
-                    topk_insert<Real, K>(L, LI, d, s_ix[q][t][r]);
-                }
-            }
-        }
-    }
-    if (seg == 0 && row) {
-        Real value = Real(0);
-        int index = -1;
-        topk_pick<Real, K>(L, LI, args.ms - 1, value, index);
-        static_cast<Real*>(args.core)[base + i] = value;
-        if (args.core_nbr) args.core_nbr[base + i] = index;
-    }
-}
-
-// Float64 rows from the materialized matrix, as hdb_core_matrix_kernel with
-// one warp per 32 rows, but the k-nearest list holds order-preserving integer
-// keys of the (non-negative) distances and moves them as 32-bit words: GB300
-// issues double compares, double selects and 64-bit integer selects to its
-// FP64 pipe, which made the double-valued list the bound of this scan.
+// 64-bit key select on 32-bit words (a 64-bit select is an FP64-pipe instruction on GB300).
 __device__ __forceinline__ unsigned long long core_key_sel(bool c, unsigned long long a, unsigned long long b) {
     const uint32_t hi = c ? (uint32_t)(a >> 32) : (uint32_t)(b >> 32);
     const uint32_t lo = c ? (uint32_t)a : (uint32_t)b;
     return ((unsigned long long)hi << 32) | lo;
 }
 
-// Ascending insertion of (d, j) with strict '<' (earlier indices first among
-// equal keys); 'below' = d < L[t] is monotone in t and carried down.
-template <int K>
-__device__ __forceinline__ void topk_insert_key(unsigned long long (&L)[K], int (&LI)[K], unsigned long long d, int j) {
-    if (!key_lt(d, L[K - 1])) return;
-    bool below = true;
-#pragma unroll
-    for (int t = K - 1; t > 0; --t) {
-        const bool below_prev = key_lt(d, L[t - 1]);
-        L[t] = core_key_sel(below_prev, L[t - 1], core_key_sel(below, d, L[t]));
-        LI[t] = below_prev ? LI[t - 1] : (below ? j : LI[t]);
-        below = below_prev;
-    }
-    L[0] = core_key_sel(below, d, L[0]);
-    LI[0] = below ? j : LI[0];
-}
-
-template <int K>
-__global__ void __launch_bounds__(kCoreMatrixRows) hdb_core_matrix_key_kernel(const CoreArgs args) {
-    using T = RealTraits<double>;
-    const int item = blockIdx.x;
-    if (item >= args.n_items) return;
-    const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
-    const int64_t base = args.offsets[w];
-    const int n = (int)(args.offsets[w + 1] - base);
-    const double* __restrict__ Dw = static_cast<const double*>(args.dist) + args.dist_offsets[w];
-    const int64_t ld = dist_ld(n);
-    const int i = r0 + threadIdx.x;
-    if (i >= n) return;
-    unsigned long long L[K];
-    int LI[K];
-#pragma unroll
-    for (int t = 0; t < K; ++t) { L[t] = T::key(T::inf()); LI[t] = -1; }
-    int j0 = 0;
-    for (; j0 + kCorePrefetch <= n; j0 += kCorePrefetch) {
-        double v[kCorePrefetch];
-#pragma unroll
-        for (int u = 0; u < kCorePrefetch; ++u) v[u] = __ldcs(Dw + (int64_t)(j0 + u) * ld + i);
-#pragma unroll
-        for (int u = 0; u < kCorePrefetch; ++u) topk_insert_key<K>(L, LI, T::key(v[u]), j0 + u);
-    }
-    for (int j = j0; j < n; ++j) topk_insert_key<K>(L, LI, T::key(__ldcs(Dw + (int64_t)j * ld + i)), j);
-    unsigned long long value = 0;
-    int index = -1;
-#pragma unroll
-    for (int t = 0; t < K; ++t)
-        if (t == args.ms - 1) { value = L[t]; index = LI[t]; }
-    static_cast<double*>(args.core)[base + i] = T::from_key(value);
-    if (args.core_nbr) args.core_nbr[base + i] = index;
-}
-
-// Rows of the materialized matrix, one warp per row, for lists of K <= 32
+// Rows of the materialized matrix, one warp per row, for lists of K <= 64
 // (both precisions).  The warp reads 32 consecutive entries of its row per
-// load (coalesced), keeps the K smallest (key, index) pairs one per lane
-// (lane t holds position t, ascending), and filters every entry with one
+// load (coalesced, eight loads in flight per lane), keeps the K smallest (key, index) pairs across the lanes
+// (position p = lane + 32*h, ascending), and filters every entry with one
 // integer compare against the current K-th key; entries below it are
-// inserted one at a time in index order by the whole warp (shift by one
-// shuffle), so the list is exactly the one the serial strict-'<' scan in
-// index order builds: the K smallest in (value, index) order.  The first 32
-// entries are placed by a warp bitonic sort on (key, index).  Keys are the
-// order-preserving bit patterns of the non-negative distances (integer
-// compares only; float64 keys compare as 32-bit word pairs).  Replaces the
-// thread-per-row scans, whose insertions diverged within the warp.
+// inserted one at a time in index order by the whole warp (each position
+// takes its predecessor by a shuffle), so the list is exactly the one the
+// serial strict-'<' scan in index order builds: the K smallest in
+// (value, index) order.  The first 32 entries are placed by a warp bitonic
+// sort on (key, index).  Keys are the order-preserving bit patterns of the
+// non-negative distances (integer compares only; float64 keys compare as
+// 32-bit word pairs).
 constexpr int kCoreRowsWarps = 8;  // warps per CTA; an item's 32 rows are shared among them
 
 template <typename Key>
@@ -615,11 +477,12 @@ __device__ __forceinline__ Key key_select(bool c, Key a, Key b) {
 
 template <typename Real, int K>
 __global__ void __launch_bounds__(32 * kCoreRowsWarps) hdb_core_rows_kernel(const CoreArgs args) {
-    static_assert(K <= 32, "one list entry per lane");
+    static_assert(K <= 64, "at most two list entries per lane");
     using T = RealTraits<Real>;
     using Key = typename T::Bits;
+    constexpr int E = (K + 31) / 32;     // list entries per lane
     constexpr Key kNone = (Key)~(Key)0;  // above every distance key (and +inf's)
-    constexpr int U = 8;                 // row loads in flight per lane
+    constexpr int U = 8;                 // row chunks per group of loads
     const int item = blockIdx.x;
     if (item >= args.n_items) return;
     const int w = args.items[2 * item], r0 = args.items[2 * item + 1];
@@ -633,22 +496,25 @@ __global__ void __launch_bounds__(32 * kCoreRowsWarps) hdb_core_rows_kernel(cons
         if (i >= n) break;  // warp-uniform
         const Real* __restrict__ row = Dw + (int64_t)i * ld;
         // First 32 entries: bitonic sort on (key, index), ascending.
-        Key lk = lane < n ? T::key(__ldcs(row + lane)) : kNone;
-        int li = lane;
+        Key lk[E];
+        int li[E];
+        lk[0] = lane < n ? T::key(__ldcs(row + lane)) : kNone;
+        li[0] = lane;
+        if constexpr (E > 1) { lk[1] = kNone; li[1] = 32 + lane; }
 #pragma unroll
         for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
             for (int j = k >> 1; j > 0; j >>= 1) {
-                const Key pk = shfl_key_xor(lk, j);
-                const int pi = __shfl_xor_sync(0xffffffffu, li, j);
-                const bool partner_less = key_lt(pk, lk) || (key_eq(pk, lk) && pi < li);
+                const Key pk = shfl_key_xor(lk[0], j);
+                const int pi = __shfl_xor_sync(0xffffffffu, li[0], j);
+                const bool partner_less = key_lt(pk, lk[0]) || (key_eq(pk, lk[0]) && pi < li[0]);
                 const bool keep_min = ((lane & k) == 0) == ((lane & j) == 0);
                 const bool take = keep_min ? partner_less : !partner_less;
-                lk = key_select(take, pk, lk);
-                li = take ? pi : li;
+                lk[0] = key_select(take, pk, lk[0]);
+                li[0] = take ? pi : li[0];
             }
         }
-        Key tau = shfl_key(lk, K - 1);
+        Key tau = shfl_key(lk[(K - 1) / 32], (K - 1) % 32);
         for (int j0 = 32; j0 < n; j0 += 32 * U) {
             Key v[U];
 #pragma unroll
@@ -665,20 +531,39 @@ __global__ void __launch_bounds__(32 * kCoreRowsWarps) hdb_core_rows_kernel(cons
                     const Key ck = shfl_key(v[u], src);
                     if (key_lt(ck, tau)) {  // warp-uniform; tau only decreases
                         const int cj = j0 + 32 * u + src;
-                        const Key pk = shfl_key_up(lk);
-                        const int pi = __shfl_up_sync(0xffffffffu, li, 1);
-                        const bool shift = lane > 0 && key_lt(ck, pk);
-                        const bool place = !shift && key_lt(ck, lk);
-                        lk = key_select(shift, pk, key_select(place, ck, lk));
-                        li = shift ? pi : (place ? cj : li);
-                        tau = shfl_key(lk, K - 1);
+                        // Predecessor of position lane + 32h: lane - 1 of the same h,
+                        // or lane 31 of h - 1 for lane 0.
+                        Key pk[E];
+                        int pi[E];
+                        pk[0] = shfl_key_up(lk[0]);
+                        pi[0] = __shfl_up_sync(0xffffffffu, li[0], 1);
+                        if constexpr (E > 1) {
+                            const Key up = shfl_key_up(lk[1]);
+                            const int upi = __shfl_up_sync(0xffffffffu, li[1], 1);
+                            const Key last = shfl_key(lk[0], 31);
+                            const int lasti = __shfl_sync(0xffffffffu, li[0], 31);
+                            pk[1] = lane == 0 ? last : up;
+                            pi[1] = lane == 0 ? lasti : upi;
+                        }
+#pragma unroll
+                        for (int h = 0; h < E; ++h) {
+                            const bool shift = (h > 0 || lane > 0) && key_lt(ck, pk[h]);
+                            const bool place = !shift && key_lt(ck, lk[h]);
+                            lk[h] = key_select(shift, pk[h], key_select(place, ck, lk[h]));
+                            li[h] = shift ? pi[h] : (place ? cj : li[h]);
+                        }
+                        tau = shfl_key(lk[(K - 1) / 32], (K - 1) % 32);
                     }
                 }
             }
         }
-        if (lane == args.ms - 1) {
-            static_cast<Real*>(args.core)[base + i] = T::from_key(lk);
-            if (args.core_nbr) args.core_nbr[base + i] = li;
+        const int pos = args.ms - 1;
+#pragma unroll
+        for (int h = 0; h < E; ++h) {
+            if (pos == lane + 32 * h) {
+                static_cast<Real*>(args.core)[base + i] = T::from_key(lk[h]);
+                if (args.core_nbr) args.core_nbr[base + i] = li[h];
+            }
         }
     }
 }

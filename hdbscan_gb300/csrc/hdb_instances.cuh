@@ -37,13 +37,7 @@ cudaError_t launch_core_points(const CoreArgs& a, int grid, cudaStream_t s, int 
 
 template <typename Real, int K>
 cudaError_t launch_core_matrix(const CoreArgs& a, int grid, cudaStream_t s, int priority) {
-    if constexpr (K <= 32)  // one warp per row, list across the lanes
-        return launch_ex(hdb_core_rows_kernel<Real, K>, grid, 32 * kCoreRowsWarps, 0, s, priority, 1, a);
-    else if constexpr (sizeof(Real) == 8)  // integer-key lists, one warp per 32 rows
-        return launch_ex(hdb_core_matrix_key_kernel<K>, grid, kCoreMatrixRows, 0, s, priority, 1, a);
-    else
-        return launch_ex(hdb_core_matrix_kernel<Real, K>, grid, kCoreMatrixRows * core_segments<Real, K>(), 0, s,
-                         priority, 1, a);
+    return launch_ex(hdb_core_rows_kernel<Real, K>, grid, 32 * kCoreRowsWarps, 0, s, priority, 1, a);
 }
 
 template <typename Real, int K, int DP>
@@ -53,12 +47,7 @@ constexpr CoreVariant core_points_variant() {
 
 template <typename Real, int K>
 constexpr CoreVariant core_matrix_variant() {
-    if constexpr (K <= 32)
-        return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_rows_kernel<Real, K>, launch_core_matrix<Real, K>};
-    else if constexpr (sizeof(Real) == 8)
-        return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_key_kernel<K>, launch_core_matrix<Real, K>};
-    else
-        return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_matrix_kernel<Real, K>, launch_core_matrix<Real, K>};
+    return CoreVariant{K, 0, kCoreMatrixRows, (const void*)hdb_core_rows_kernel<Real, K>, launch_core_matrix<Real, K>};
 }
 
 template <typename Real>
@@ -91,7 +80,7 @@ cudaError_t launch_prepare(const void* X, int input_type, void* out, int64_t poi
 
 template <typename Real>
 cudaError_t launch_backward(const BackwardArgs& a, int grid, cudaStream_t s, int priority) {
-    return launch_ex(hdb_backward_kernel<Real>, grid, 256, 0, s, priority, 1, a);
+    return launch_ex(hdb_backward_kernel<Real>, grid, 32 * kBackwardWarps, 0, s, priority, 1, a);
 }
 
 // Two arenas (Prim/tree overlap) when they fit next to the staged window,

@@ -26,6 +26,8 @@
 //  * linkage uses union by size over packed 32-bit word pairs
 //    {parent | component node << 16, size} without path compression;
 //    the roots, hence the tree, are those of the reference's union-find.
+//    Batches of 32 edges find their roots in parallel, then one lane
+//    commits the unions in order (fixing up roots merged within the batch).
 //  * condensation runs the reference's breadth-first queue one level at a
 //    time across the warp: every cluster is a path of the dendrogram (it only
 //    branches where it ends in a split), so the nodes of one level belong to
@@ -262,6 +264,20 @@ __device__ int partition_warp(SortPair<Real>* p, int lo, int hi, int16_t* list_a
     return i;
 }
 
+// Lanes holding the same 8-bit digit (bit 8 marks an invalid lane, whose
+// mask is never used): one ballot per digit bit, each lane keeping the lanes
+// that agree with it on every bit (the warp multisplit form of match.any,
+// which is far slower on this GPU).
+__device__ __forceinline__ unsigned same_digit_lanes(int d) {
+    unsigned same = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 9; ++b) {
+        const unsigned bits = __ballot_sync(0xffffffffu, (d >> b) & 1);
+        same &= ((d >> b) & 1) ? bits : ~bits;
+    }
+    return same;
+}
+
 __device__ __forceinline__ int radix_digit(uint32_t k, int shift) { return (int)((k >> shift) & 0xffu); }
 __device__ __forceinline__ int radix_digit(unsigned long long k, int shift) {
     const uint32_t w = shift < 32 ? (uint32_t)k : (uint32_t)(k >> 32);
@@ -294,7 +310,7 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
         for (int base = 0; base < m; base += 32) {
             const int i = base + lane;
             const int d = i < m ? radix_digit(kin[i], shift) : 256;
-            const unsigned same = __match_any_sync(0xffffffffu, d);
+            const unsigned same = same_digit_lanes(d);
             if (d < 256 && (same & lt) == 0) hist[d] += __popc(same);
             __syncwarp();
         }
@@ -318,7 +334,7 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
             const bool valid = i < m;
             const Key k = valid ? kin[i] : Key(0);
             const int d = valid ? radix_digit(k, shift) : 256;
-            const unsigned same = __match_any_sync(0xffffffffu, d);
+            const unsigned same = same_digit_lanes(d);
             int pos = 0;
             if (valid) pos = hist[d] + __popc(same & lt);
             __syncwarp();
@@ -345,12 +361,12 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
 }
 
 // Sorts r0[0..m) with NumPy's quicksort order; leaves the order in s2 and the
-// sorted weights in r0.  Whole-warp call.  try_radix: attempt the tie-free
-// radix path first (worth it where ties are rare: min_samples <= 2).
+// sorted weights in r0.  Whole-warp call.  try_distinct: attempt the
+// tie-free radix path first (worth it where ties are rare: min_samples <= 2).
 template <typename Real>
-__device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
+__device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_distinct) {
     const int lane = threadIdx.x & 31;
-    if (try_radix && m >= 256 && radix_sort_distinct_warp<Real>(a, m)) return;
+    if (try_distinct && m >= 256 && radix_sort_distinct_warp<Real>(a, m)) return;
     SortPair<Real>* p = reinterpret_cast<SortPair<Real>*>(a.r1);
     for (int i = lane; i < m; i += 32) { p[i].w = a.r0[i]; p[i].idx = i; }
     int16_t *task_lo = a.s5, *task_hi = a.s6, *task_depth = a.s7;  // depth*2 + checked
@@ -406,37 +422,64 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_radix) {
 // Single linkage (reference: _kernels.py:518-556).  Node n+i merges the
 // components of the i-th sorted edge (source side first).  Inputs: s2 sorted
 // sources, s3 sorted targets.  Outputs: s4 left, s5 right, s6 size of node n+i
-// at index i.  Lane 0 runs the union-find; the words live in r1/r2.
+// at index i.  The words live in r1/r2; s7/s8 hold a batch's roots.
+//
+// Edges go in batches of 32: first every lane walks its edge's two endpoints
+// to their roots in the state before the batch (in parallel), then lane 0
+// commits the batch's unions in order, reading each root's word (which it
+// needs anyway for the node id and size) and following parents only from a
+// root that an earlier union of the same batch made a child.  Only roots'
+// words ever change, so the committed roots, sizes, orientations and node ids
+// are those of the serial union-find.
 // ---------------------------------------------------------------------------
 template <typename Real>
 __device__ void linkage_warp(const Arena<Real>& a, int n) {
     const int lane = threadIdx.x & 31;
+    const int m = n - 1;
     uint2* U = reinterpret_cast<uint2*>(a.r1);  // {parent | node << 16, size}
+    int16_t* root_x = a.s7;
+    int16_t* root_y = a.s8;
     for (int x = lane; x < n; x += 32) U[x] = make_uint2((uint32_t)x | ((uint32_t)x << 16), 1u);
     __syncwarp();
-    if (lane == 0) {
-        int xn = a.s2[0], yn = a.s3[0];  // n >= 2: at least one edge
-        for (int i = 0; i < n - 1; ++i) {
-            int x = xn, y = yn;
-            if (i + 2 < n) { xn = a.s2[i + 1]; yn = a.s3[i + 1]; }  // next endpoints, off the critical path
-            uint2 wx = U[x], wy = U[y];
-            while ((int)(wx.x & 0xffffu) != x) { x = (int)(wx.x & 0xffffu); wx = U[x]; }
-            while ((int)(wy.x & 0xffffu) != y) { y = (int)(wy.x & 0xffffu); wy = U[y]; }
-            const uint32_t sx = wx.y, sy = wy.y, s = sx + sy;
-            a.s4[i] = (int16_t)(wx.x >> 16);
-            a.s5[i] = (int16_t)(wy.x >> 16);
-            a.s6[i] = (int16_t)s;
-            const uint32_t node = (uint32_t)(n + i) << 16;
-            if (sx < sy) {
-                U[x].x = (wx.x & 0xffff0000u) | (uint32_t)y;
-                U[y] = make_uint2((uint32_t)y | node, s);
-            } else {
-                U[y].x = (wy.x & 0xffff0000u) | (uint32_t)x;
-                U[x] = make_uint2((uint32_t)x | node, s);
+    for (int base = 0; base < m; base += 32) {
+        const int i = base + lane;
+        if (i < m) {
+            int x = a.s2[i], y = a.s3[i];
+            uint32_t px = U[x].x & 0xffffu, py = U[y].x & 0xffffu;
+            while ((int)px != x || (int)py != y) {
+                x = (int)px;
+                y = (int)py;
+                px = U[x].x & 0xffffu;
+                py = U[y].x & 0xffffu;
+            }
+            root_x[lane] = (int16_t)x;
+            root_y[lane] = (int16_t)y;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const int count = min(32, m - base);
+            for (int l = 0; l < count; ++l) {
+                int x = root_x[l], y = root_y[l];
+                uint2 wx = U[x], wy = U[y];
+                while ((int)(wx.x & 0xffffu) != x) { x = (int)(wx.x & 0xffffu); wx = U[x]; }
+                while ((int)(wy.x & 0xffffu) != y) { y = (int)(wy.x & 0xffffu); wy = U[y]; }
+                const int e = base + l;
+                const uint32_t sx = wx.y, sy = wy.y, s = sx + sy;
+                a.s4[e] = (int16_t)(wx.x >> 16);
+                a.s5[e] = (int16_t)(wy.x >> 16);
+                a.s6[e] = (int16_t)s;
+                const uint32_t node = (uint32_t)(n + e) << 16;
+                if (sx < sy) {
+                    U[x].x = (wx.x & 0xffff0000u) | (uint32_t)y;
+                    U[y] = make_uint2((uint32_t)y | node, s);
+                } else {
+                    U[y].x = (wy.x & 0xffff0000u) | (uint32_t)x;
+                    U[x] = make_uint2((uint32_t)x | node, s);
+                }
             }
         }
+        __syncwarp();
     }
-    __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
