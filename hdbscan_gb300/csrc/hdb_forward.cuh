@@ -446,7 +446,6 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
     __shared__ WindowMeta s_meta[2];
 
     const int tid = threadIdx.x;
-    const int lane = tid & 31;
     const int warp = tid >> 5;
     const Real* __restrict__ X = static_cast<const Real*>(args.X);
     const int D = args.D;
@@ -499,7 +498,24 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
         // ---- stage coordinates / cores, validate input -----------------------
         int bad = 0;
         if (xs) {
-            for (int t = tid; t < n * DPS; t += PT) {
+            // Eight independent loads in flight per thread before the stores.
+            constexpr int U = 8;
+            const int total = n * DPS;
+            int t = tid;
+            for (; t + (U - 1) * PT < total; t += U * PT) {
+                Real v[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int tt = t + u * PT, j = tt / DPS, kk = tt - j * DPS;
+                    v[u] = kk < D ? Xw[(int64_t)j * D + kk] : Real(0);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    bad |= !isfinite(v[u]);
+                    s_x[t + u * PT] = v[u];
+                }
+            }
+            for (; t < total; t += PT) {
                 const int j = t / DPS, kk = t - j * DPS;
                 Real v = Real(0);
                 if (kk < D) { v = Xw[(int64_t)j * D + kk]; bad |= !isfinite(v); }
