@@ -128,3 +128,22 @@ def test_long_core_lists_match_oracle(cuda, precision, ms):
     # split into column ranges, float64 scans on integer keys; duplicated
     # points give tied core distances.
     _compare(_windows(ms, 6, (ms + 10, 900), 6), 8, ms, 0.0, precision, force_matrix=True)
+
+
+def _nested_pairs(pairs, seed):
+    """Tight pairs of points on a line with growing gaps: every merge up the
+    dendrogram joins a pair (two points) to everything below it, so with
+    min_cluster_size 2 each split's large child splits again - clusters nested
+    `pairs` levels deep."""
+    rng = np.random.default_rng(seed)
+    centres = np.cumsum(1.0 + 0.05 * np.arange(pairs)) * 10.0
+    x = np.repeat(centres, 2)[:, None] + rng.normal(0, 0.01, (2 * pairs, 1))
+    return np.concatenate([x, rng.normal(0, 0.01, (2 * pairs, 2))], axis=1)
+
+
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+@pytest.mark.parametrize("pairs", [40, 90])
+def test_deeply_nested_clusters_match_oracle(cuda, precision, pairs):
+    # Cluster trees 40 and 90 splits deep: the breadth-first condensation runs
+    # one long queue level per split with exactly two nodes in it.
+    _compare([_nested_pairs(pairs, pairs), _nested_pairs(pairs, pairs + 1)[::-1].copy()], 2, 1, 0.0, precision)
