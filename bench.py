@@ -518,7 +518,8 @@ def main():
         end.record(stream)
         end.synchronize()
         plain_ms.append(start.elapsed_time(end))
-    plain_value = whole_job_rate(B, world, reduce_max(float(np.mean(plain_ms)), world, device))
+    plain_value = (whole_job_rate(B, world, reduce_max(float(np.mean(plain_ms)), world, device))
+                   if plain_ms else None)
     plain_exact = bool(np.array_equal(plain_labels.cpu().numpy(), graph_labels))
 
     # ---- end to end through the public API ----------------------------------
@@ -627,7 +628,7 @@ def main():
                    "l2": "256 MiB flush between timed steps", "graph": True, "parallelism": "replicas"},
         "points_per_s": T * world / (ms_per_step / 1e3),
         "plain_per_window": {"value": plain_value, "unit": "windows/s", "labels_bit_exact": plain_exact},
-        "speedup_vs_plain": value / plain_value,
+        "speedup_vs_plain": value / plain_value if plain_value else None,
         "labels_bit_exact": {"graph_vs_oracle_sample": oracle_exact, "e2e_vs_graph": e2e_exact},
         "e2e": {"value": e2e_value, "unit": "windows/s", "h2d_bytes_per_step": int(host.nbytes),
                 "d2h_bytes_per_step": int(T * 4 + (host.itemsize if backward else 4))},

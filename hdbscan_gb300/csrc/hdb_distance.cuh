@@ -147,9 +147,10 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
                 }
             };
             if (int_square) {
-                // Squares on the integer pipes (hdb_exact.h); half of the
-                // running sums (pairs with a + b odd) add on the integer pipes
-                // too, the other half on the FP64 pipe, which balances them.
+                // Squares on the integer pipes (hdb_exact.h); 10 of the 16
+                // running sums add on the integer pipes too, the other 6 on
+                // the FP64 pipe, which balances the two (8 or 12 of 16 is
+                // slower).
                 for (int k = 0; k < kend; ++k) {
                     Real xi[4], xj[4];
                     DistVec<Real>::load4(&s_i[k][ty * 4], xi);
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
                             const Real sq = T::sqr(T::sub(xi[a], xj[b]));
-                            acc[a][b] = ((a + b) & 1) ? add_rn_nonneg(acc[a][b], sq) : T::add(acc[a][b], sq);
+                            acc[a][b] = ((((a * 4 + b) * 5) & 15) < 10) ? add_rn_nonneg(acc[a][b], sq) : T::add(acc[a][b], sq);
                         }
                 }
             } else {

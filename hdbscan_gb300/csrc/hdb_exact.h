@@ -7,7 +7,7 @@
 // rounded (round-to-nearest-even) square of d computed with 32x32->64-bit
 // integer products, so the square moves to the integer pipes; add_rn_nonneg
 // (end of this file) does the same for the running sum, which the distance
-// kernel applies to half of its accumulators so that the FP64 pipe and the
+// kernel applies to 10 of its 16 accumulators so that the FP64 pipe and the
 // integer pipes carry balanced loads.  The square's result is
 // bit-identical to d*d under IEEE-754 for every input: zero returns +0, and
 // values whose square is not a normal double (|d| < 2^-511 or |d| >= 2^511,
@@ -22,7 +22,10 @@
 //   normalised to have its top bit at 105, the top 53 bits are rounded to
 //   nearest-even on the remaining 53 bits, and the biased exponent of d^2 is
 //   2e - 1023 (+1 when m^2 >= 2^105); a rounding carry into bit 53 moves into
-//   the exponent field by the addition that packs the result.
+//   the exponent field by the addition that packs the result.  On the device
+//   the three products are mul.wide.u32, the 128-bit sum one add.cc/addc
+//   chain, and normalising and extracting the significand one funnel shift
+//   per word.
 // Usable from host code (tests compare it with the host's multiply).
 #pragma once
 #include <cstdint>
@@ -61,8 +64,7 @@ HDB_HD double exact_double(uint64_t b) {
 // the square is written with 32-bit operations only.
 HDB_HD void mul_wide(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
 #ifdef __CUDA_ARCH__
-    lo = a * b;
-    hi = __umulhi(a, b);
+    asm("{\n\t.reg .b64 t;\n\tmul.wide.u32 t, %2, %3;\n\tmov.b64 {%0, %1}, t;\n\t}" : "=r"(lo), "=r"(hi) : "r"(a), "r"(b));
 #else
     const uint64_t p = (uint64_t)a * (uint64_t)b;
     lo = (uint32_t)p;
@@ -77,6 +79,32 @@ HDB_HD uint32_t add_carry(uint32_t a, uint32_t b, uint32_t carry_in, uint32_t& c
     const uint32_t r = t + carry_in;
     carry_out = c1 | (r < t ? 1u : 0u);
     return r;
+}
+
+// (hi:lo) += (bh:bl), two-word add with the carry between the words.
+HDB_HD void add2(uint32_t& lo, uint32_t& hi, uint32_t bl, uint32_t bh) {
+#ifdef __CUDA_ARCH__
+    asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(lo), "+r"(hi) : "r"(bl), "r"(bh));
+#else
+    uint32_t c;
+    lo = add_carry(lo, bl, 0u, c);
+    hi = hi + bh + c;
+#endif
+}
+
+// (w3:w2:w1) = (c:b2:b1) + (0:a2:a1), three-word add with carries.
+HDB_HD void add3(uint32_t a1, uint32_t b1, uint32_t a2, uint32_t b2, uint32_t c, uint32_t& w1, uint32_t& w2,
+                 uint32_t& w3) {
+#ifdef __CUDA_ARCH__
+    asm("add.cc.u32 %0, %3, %4;\n\taddc.cc.u32 %1, %5, %6;\n\taddc.u32 %2, %7, 0;"
+        : "=r"(w1), "=r"(w2), "=r"(w3)
+        : "r"(a1), "r"(b1), "r"(a2), "r"(b2), "r"(c));
+#else
+    uint32_t c1, c2;
+    w1 = add_carry(a1, b1, 0u, c1);
+    w2 = add_carry(a2, b2, c1, c2);
+    w3 = c + c2;
+#endif
 }
 
 // (hi:lo) >> s for 0 <= s < 32, low word.
@@ -110,27 +138,20 @@ HDB_HD double sqr_rn_words(uint32_t hi, uint32_t lo, bool zero) {
     mul_wide(mh, ml, p1h, p1l);  // mh*ml < 2^53
     mul_wide(mh, mh, p2h, p2l);  // mh^2 < 2^42
     // S = m^2 = p2 * 2^64 + p1 * 2^33 + p0 in words w3:w2:w1:w0.
-    uint32_t c1, c2, unused;
+    uint32_t w1, w2, w3;
+    add3(p0h, p1l << 1, p2l, (p1h << 1) | (p1l >> 31), p2h, w1, w2, w3);
     const uint32_t w0 = p0l;
-    const uint32_t w1 = add_carry(p0h, p1l << 1, 0u, c1);
-    const uint32_t w2 = add_carry(p2l, (p1h << 1) | (p1l >> 31), c1, c2);
-    const uint32_t w3 = add_carry(p2h, 0u, c2, unused);
-    const uint32_t top = (w3 >> 9) & 1u;  // S >= 2^105 (bit 105 = bit 9 of w3)
-    const uint32_t sh = 1u - top;         // normalise: top bit at 105
-    const uint32_t v3 = funnel_left(w2, w3, sh);
-    const uint32_t v2 = funnel_left(w1, w2, sh);
-    const uint32_t v1 = funnel_left(w0, w1, sh);
-    const uint32_t v0 = w0 << sh;
-    // Significand = S >> 53: bits 53..84 (low word) and 85..105 (high, hidden bit at 20).
-    uint32_t mlo = funnel_right(v1, v2, 21);
-    uint32_t mhi = funnel_right(v2, v3, 21) & 0x1fffffu;
-    // Remainder S mod 2^53: round bit = bit 52 (bit 20 of v1), sticky = bits 0..51.
-    const uint32_t round_bit = (v1 >> 20) & 1u;
-    const uint32_t sticky = (v1 & 0xfffffu) | v0;
+    // S in [2^104, 2^106); top = bit 105 (bit 9 of w3).  The significand is
+    // S >> (52 + top) (53 bits, hidden bit at 52), the round bit is bit
+    // 51 + top and the sticky bits are the ones below it.
+    const uint32_t top = (w3 >> 9) & 1u;
+    const uint32_t sh = 20u + top;
+    uint32_t mlo = funnel_right(w1, w2, sh);
+    uint32_t mhi = funnel_right(w2, w3, sh) & 0x1fffffu;
+    const uint32_t round_bit = (w1 >> (sh - 1u)) & 1u;
+    const uint32_t sticky = (w1 & ((1u << (sh - 1u)) - 1u)) | w0;
     const uint32_t up = round_bit & ((sticky != 0u ? 1u : 0u) | (mlo & 1u));
-    uint32_t carry;
-    mlo = add_carry(mlo, up, 0u, carry);
-    mhi += carry;
+    add2(mlo, mhi, up, 0u);
     // Biased exponent E = 2e - 1023 + top; (E - 1) << 20 plus the high word
     // (hidden bit included) packs it, a carry to 2^53 bumping the exponent.
     const uint32_t rhi = zero ? 0u : ((2u * e - 1024u + top) << 20) + mhi;
@@ -229,9 +250,8 @@ HDB_HD void add_rn_nonneg_words(uint32_t ahi, uint32_t alo, uint32_t bhi, uint32
         lost = 1u;
     }
     al |= lost != 0u ? 1u : 0u;
-    uint32_t c;
-    uint32_t sl = add_carry(xl, al, 0u, c);
-    uint32_t sh = xh + ah + c;
+    uint32_t sl = xl, sh = xh;
+    add2(sl, sh, al, ah);
     uint32_t e = ex;
     if (sh >> 24) {  // carry out of the 56 bits: one sticky shift
         sl = funnel_right(sl, sh, 1u) | (sl & 1u);
@@ -242,8 +262,7 @@ HDB_HD void add_rn_nonneg_words(uint32_t ahi, uint32_t alo, uint32_t bhi, uint32
     uint32_t mh = sh >> 3;  // 21 bits, hidden bit at 20
     const uint32_t guard = (sl >> 2) & 1u, sticky = sl & 3u;
     const uint32_t up = guard & ((sticky != 0u ? 1u : 0u) | (ml & 1u));
-    ml = add_carry(ml, up, 0u, c);
-    mh += c;
+    add2(ml, mh, up, 0u);
     uint32_t hi = ((e - 1u) << 20) + mh;
     uint32_t lo = ml;
     if (hi >= 0x7ff00000u || fx == 0x7ffu) { hi = 0x7ff00000u; lo = 0u; }  // overflow or an infinite operand
