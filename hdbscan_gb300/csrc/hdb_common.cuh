@@ -58,9 +58,10 @@ template <> struct RealTraits<double> {
     __device__ __forceinline__ static double mul(double a, double b) { return __dmul_rn(a, b); }
     // Correctly rounded a*a of a difference of operand_safe values, on the
     // integer pipes (hdb_exact.h): the FP64 pipe then carries only the
-    // subtraction and the addition.
+    // subtraction and the addition.  operand_safe is the domain of the fused
+    // integer square-and-add (sqr_add_rn), a subset of sqr_rn_safe's.
     __device__ __forceinline__ static double sqr(double a) { return sqr_rn_safe(a); }
-    __device__ __forceinline__ static bool operand_safe(double x) { return sqr_operand_safe(x); }
+    __device__ __forceinline__ static bool operand_safe(double x) { return sqr_add_operand_safe(x); }
     __device__ __forceinline__ static double mul_ru(double a, double b) { return __dmul_ru(a, b); }
     __device__ __forceinline__ static double add(double a, double b) { return __dadd_rn(a, b); }
     __device__ __forceinline__ static double sqrt_rn(double a) { return __dsqrt_rn(a); }

@@ -102,7 +102,15 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
             }
         }
         // Chunk-uniform choice of the square: the integer-pipe one when every
-        // staged coordinate keeps all squares normal, else the hardware multiply.
+        // staged coordinate keeps all squares normal and every float64
+        // accumulator is in the fused square-and-add's domain (hdb_exact.h),
+        // else the hardware multiply.
+        if constexpr (sizeof(Real) == 8) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) safe = safe && sqr_add_acc_safe(acc[a][b]);
+        }
         const bool int_square = __syncthreads_and(safe);
         const int kend = min(KC, D - k0);
         if constexpr (sizeof(Real) == 4) {
@@ -147,10 +155,11 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
                 }
             };
             if (int_square) {
-                // Squares on the integer pipes (hdb_exact.h); 10 of the 16
-                // running sums add on the integer pipes too, the other 6 on
-                // the FP64 pipe, which balances the two (8 or 12 of 16 is
-                // slower).
+                // Squares on the integer pipes (hdb_exact.h); 12 of the 16
+                // running sums add on the integer pipes too, fused with their
+                // square (sqr_add_rn: the square is never packed), the other
+                // 4 on the FP64 pipe, which balances the two pipes (10, 13,
+                // 14 or 16 of 16 is slower).
                 for (int k = 0; k < kend; ++k) {
                     Real xi[4], xj[4];
                     DistVec<Real>::load4(&s_i[k][ty * 4], xi);
@@ -159,8 +168,9 @@ __global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs ar
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
                         for (int b = 0; b < 4; ++b) {
-                            const Real sq = T::sqr(T::sub(xi[a], xj[b]));
-                            acc[a][b] = ((((a * 4 + b) * 5) & 15) < 10) ? add_rn_nonneg(acc[a][b], sq) : T::add(acc[a][b], sq);
+                            const Real delta = T::sub(xi[a], xj[b]);
+                            acc[a][b] = (((a * 4 + b) & 3) != 0) ? sqr_add_rn(acc[a][b], delta)
+                                                                 : T::add(acc[a][b], T::sqr(delta));
                         }
                 }
             } else {

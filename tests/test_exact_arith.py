@@ -1,9 +1,11 @@
-"""The integer-pipe binary64 square and addition (hdbscan_gb300/csrc/hdb_exact.h)
-against the host's IEEE multiply and add, bit for bit: random bit patterns
-over every exponent, the exponent boundaries of the fast path, rounding
-carries and halfway cases, zeros, subnormals, infinities and NaN (square);
-non-negative operands of every class and exponent gap, carries, halfway cases
-and overflow (addition)."""
+"""The integer-pipe binary64 square and fused square-and-add
+(hdbscan_gb300/csrc/hdb_exact.h) against the host's and the device's IEEE
+multiply and add, bit for bit: random bit patterns over every exponent, the
+exponent boundaries of the fast path, rounding carries and halfway cases,
+zeros, subnormals, infinities and NaN (square); accumulators and differences
+over the fused operation's whole domain, close exponents, exact and halfway
+squares, zeros and k-ordered chains as the distance kernel runs them
+(square-and-add)."""
 
 import shutil
 import subprocess
@@ -172,7 +174,7 @@ def test_device_integer_square_matches_dmul(cuda, tmp_path):
     assert "mismatches 0" in result.stdout
 
 
-ADD_PROGRAM = r"""
+FUSED_PROGRAM = r"""
 #include <cstdio>
 #include <cstdint>
 #include <cstdlib>
@@ -182,50 +184,83 @@ ADD_PROGRAM = r"""
 using namespace hdb;
 
 static uint64_t count = 0, bad = 0;
-static void check(double a, double b) {
-    volatile double va = a, vb = b;
-    const double want = va + vb;  // host IEEE add
-    const double got = add_rn_nonneg(a, b);
+static void check(double acc, double d) {
+    volatile double va = acc, vd = d;
+    volatile double sq = vd * vd;
+    const double want = va + sq;  // host IEEE multiply, then add
+    const double got = sqr_add_rn(acc, d);
     ++count;
     if (exact_bits(want) != exact_bits(got)) {
-        if (bad < 10) std::printf("mismatch a=%a b=%a want=%a got=%a\n", a, b, want, got);
+        if (bad < 10) std::printf("mismatch acc=%a d=%a want=%a got=%a\n", acc, d, want, got);
         ++bad;
     }
 }
 
 int main(int argc, char** argv) {
     const long n = argc > 1 ? std::atol(argv[1]) : 1000000;
-    std::mt19937_64 rng(20261204);
+    std::mt19937_64 rng(20261205);
     const unsigned long long frac = (1ull << 52) - 1;
-    auto with_exp = [&](unsigned long long e) { return exact_double((e << 52) | (rng() & frac)); };
-    for (long i = 0; i < n; ++i) check(with_exp(1 + rng() % 2046), with_exp(1 + rng() % 2046));  // any gap
-    for (long i = 0; i < n; ++i) {                                                                 // close exponents
-        const unsigned long long e = 1 + rng() % 2040;
-        const long long f = (long long)e - (long long)(rng() % 60);
-        const double a = with_exp(e), b = with_exp(f < 1 ? 1ull : (unsigned long long)f);
-        check(a, b);
-        check(b, a);
-    }
-    for (long i = 0; i < n; ++i) {  // any non-negative non-NaN pattern, subnormals included
-        const double a = exact_double(rng() >> 1), b = exact_double((rng() >> 1) & ((i & 1) ? ~0ull : ((1ull << 56) - 1)));
-        if (std::isnan(a) || std::isnan(b)) continue;
-        check(a, b);
-    }
-    for (long i = 0; i < n / 4; ++i) check(with_exp(2000 + rng() % 47), with_exp(1995 + rng() % 52));  // overflow
-    // Halfway and carry patterns at every exponent gap.
-    for (unsigned long long e = 60; e < 2040; e += 37)
-        for (unsigned long long d = 0; d < 60; ++d)
-            for (unsigned long long fa : {0ull, 1ull, 2ull, 3ull, frac, 1ull << 51})
-                for (unsigned long long fb : {0ull, 1ull, frac, 1ull << 51, (1ull << 51) + 1, 1ull << 50}) {
-                    const double a = exact_double((e << 52) | fa), b = exact_double(((e - d) << 52) | fb);
-                    check(a, b);
-                    check(b, a);
-                }
-    for (double a : {0.0, 0x1p-1074, 0x1p-1022, 1.0, (double)INFINITY, 0x1.fffffffffffffp+1023})
-        for (double b : {0.0, 0x1p-1074, 0x1p-1022, 1.0, 0x1p+1023, 0x1.fffffffffffffp+1022, (double)INFINITY}) {
-            check(a, b);
-            check(b, a);
+    auto make = [&](unsigned long long e, unsigned long long f, bool neg) {
+        return exact_double(((unsigned long long)neg << 63) | (e << 52) | (f & frac));
+    };
+    // The domain: d = 0 or |d| in [2^-511, 2^501] (biased exponents 512..1524),
+    // acc = +0 or normal below 2^1008 (biased exponents 1..2030).
+    auto any_d = [&]() { return make(512 + rng() % 1013, rng(), rng() & 1); };
+    auto any_acc = [&]() { return make(1 + rng() % 2030, rng(), false); };
+    for (long i = 0; i < n; ++i) check(any_acc(), any_d());
+    for (long i = 0; i < 2 * n; ++i) {  // accumulator exponent within 65 of the square's
+        const double d = any_d();
+        const long long eq = 2 * (long long)((exact_bits(d) >> 52) & 0x7ff) - 1023;
+        long long ea = eq + (long long)(rng() % 131) - 65;
+        ea = ea < 1 ? 1 : (ea > 2030 ? 2030 : ea);
+        unsigned long long f = rng();
+        switch (rng() % 4) {
+            case 1: f = frac; break;
+            case 2: f &= 0xffffff; break;
+            case 3: f = (f & ~0xffffffull) | (1ull << (rng() % 52)); break;
+            default: break;
         }
+        check(make((unsigned long long)ea, f, false), d);
+    }
+    for (long i = 0; i < n; ++i) {  // exact and halfway squares: short significands of d
+        const unsigned long long e = 512 + rng() % 1013;
+        unsigned long long f = (rng() & ((1ull << 27) - 1)) << 25;
+        if (rng() & 1) f |= 1ull << (rng() % 25);
+        const long long eq = 2 * (long long)e - 1023;
+        long long ea = eq + (long long)(rng() % 121) - 60;
+        ea = ea < 1 ? 1 : (ea > 2030 ? 2030 : ea);
+        unsigned long long fa = rng();
+        if (rng() & 1) fa &= ~((1ull << (rng() % 52)) - 1);
+        check(make((unsigned long long)ea, fa, false), make(e, f, rng() & 1));
+    }
+    for (long i = 0; i < n / 10; ++i) {  // zeros
+        check(0.0, any_d());
+        check(any_acc(), 0.0);
+        check(any_acc(), -0.0);
+    }
+    for (double d : {0.0, -0.0, 0x1p-511, -0x1p-511, 0x1p501, -0x1p501, 0x1.fffffffffffffp500, 0x1.0000000000001p-511})
+        for (double a : {0.0, 0x1p-1022, 0x1.fffffffffffffp999, 0x1.fffffffffffffp1006, 1.0, 0x1.8p-1000}) check(a, d);
+    // k-ordered chains of squared differences, as the distance kernel runs them.
+    for (long i = 0; i < n / 20; ++i) {
+        const int D = 1 + (int)(rng() % 128), scale = (int)(rng() % 200) - 100;
+        std::normal_distribution<double> normal(0.0, 1.0);
+        double acc = 0.0;
+        volatile double want = 0.0;
+        for (int k = 0; k < D; ++k) {
+            const double xi = std::ldexp(normal(rng), scale);
+            const double xj = (rng() % 16 == 0) ? xi : std::ldexp(normal(rng), scale);
+            volatile double vi = xi, vj = xj;
+            volatile double d = vi - vj;
+            volatile double sq = d * d;
+            want = want + sq;
+            acc = sqr_add_rn(acc, d);
+        }
+        ++count;
+        if (exact_bits(acc) != exact_bits((double)want)) {
+            if (bad < 10) std::printf("chain mismatch D=%d\n", D);
+            ++bad;
+        }
+    }
     std::printf("checked %llu mismatches %llu\n", (unsigned long long)count, (unsigned long long)bad);
     return bad != 0;
 }
@@ -233,10 +268,10 @@ int main(int argc, char** argv) {
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
-def test_integer_add_matches_ieee_add(tmp_path):
-    src = tmp_path / "add.cpp"
-    src.write_text(ADD_PROGRAM)
-    exe = tmp_path / "add"
+def test_fused_square_add_matches_ieee(tmp_path):
+    src = tmp_path / "fused.cpp"
+    src.write_text(FUSED_PROGRAM)
+    exe = tmp_path / "fused"
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
                     "-I", str(ROOT / "hdbscan_gb300" / "csrc"), str(src), "-o", str(exe)], check=True)
     result = subprocess.run([str(exe), "1000000"], capture_output=True, text=True)
@@ -245,7 +280,7 @@ def test_integer_add_matches_ieee_add(tmp_path):
     assert int(result.stdout.split("checked ")[1].split()[0]) > 4_000_000
 
 
-DEVICE_ADD_PROGRAM = r"""
+DEVICE_FUSED_PROGRAM = r"""
 #include <cstdio>
 #include <cstdint>
 #include <random>
@@ -257,9 +292,9 @@ using namespace hdb;
 __global__ void compare(const unsigned long long* in, unsigned long long* bad, unsigned long long* first, long n) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double a = __longlong_as_double((long long)in[2 * i]), b = __longlong_as_double((long long)in[2 * i + 1]);
-    const double want = __dadd_rn(a, b);
-    const double got = add_rn_nonneg(a, b);
+    const double acc = __longlong_as_double((long long)in[2 * i]), d = __longlong_as_double((long long)in[2 * i + 1]);
+    const double want = __dadd_rn(acc, __dmul_rn(d, d));
+    const double got = sqr_add_rn(acc, d);
     if (__double_as_longlong(want) != __double_as_longlong(got)) {
         if (atomicAdd(bad, 1ull) == 0ull) *first = (unsigned long long)i;
     }
@@ -268,21 +303,24 @@ __global__ void compare(const unsigned long long* in, unsigned long long* bad, u
 int main() {
     const long n = 1l << 23;
     std::vector<unsigned long long> host(2 * n);
-    std::mt19937_64 rng(11);
+    std::mt19937_64 rng(12);
     const unsigned long long frac = (1ull << 52) - 1;
     for (long i = 0; i < n; ++i) {
-        unsigned long long a, b;
-        switch (i & 3) {
-            case 0: a = rng() >> 1; b = rng() >> 1; break;                                     // any non-negative
-            case 1: a = ((1 + rng() % 2046) << 52) | (rng() & frac); b = ((1 + rng() % 2046) << 52) | (rng() & frac); break;
-            case 2: { const unsigned long long e = 60 + rng() % 1980; a = (e << 52) | (rng() & frac);
-                      b = ((e - rng() % 58) << 52) | (rng() & frac); break; }                       // close exponents
-            default: a = (rng() & 1) ? 0ull : (rng() & frac); b = rng() & frac; break;             // zero, subnormal
+        const unsigned long long ed = 512 + rng() % 1013;
+        unsigned long long d = ((rng() & 1) << 63) | (ed << 52) | (rng() & frac), a;
+        if ((i & 3) == 3) d &= ~((1ull << (25 + rng() % 27)) - 1);  // short significands: exact and halfway squares
+        if (i % 64 == 5) d = (rng() & 1) << 63;                      // zero difference
+        long long ea;
+        if (i & 1) {
+            ea = 2 * (long long)ed - 1023 + (long long)(rng() % 131) - 65;  // close exponents
+        } else {
+            ea = 1 + (long long)(rng() % 2030);
         }
-        if (((a >> 52) & 0x7ff) == 0x7ff && (a & frac)) a = 0;  // no NaN operands
-        if (((b >> 52) & 0x7ff) == 0x7ff && (b & frac)) b = 0;
+        ea = ea < 1 ? 1 : (ea > 2030 ? 2030 : ea);
+        a = ((unsigned long long)ea << 52) | (rng() & frac);
+        if (i % 64 == 9) a = 0;  // zero accumulator
         host[2 * i] = a;
-        host[2 * i + 1] = b;
+        host[2 * i + 1] = d;
     }
     unsigned long long *d_in, *d_bad, *d_first;
     cudaMalloc(&d_in, 2 * n * sizeof(unsigned long long));
@@ -304,11 +342,11 @@ int main() {
 
 
 @pytest.mark.gpu
-def test_device_integer_add_matches_dadd(cuda, tmp_path):
+def test_device_fused_square_add_matches_hardware(cuda, tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    src = tmp_path / "add_device.cu"
-    src.write_text(DEVICE_ADD_PROGRAM)
-    exe = tmp_path / "add_device"
+    src = tmp_path / "fused_device.cu"
+    src.write_text(DEVICE_FUSED_PROGRAM)
+    exe = tmp_path / "fused_device"
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "--fmad=false", "-std=c++17",
                     "-I", str(ROOT / "hdbscan_gb300" / "csrc"), str(src), "-o", str(exe)], check=True)
     result = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
