@@ -56,8 +56,10 @@ template <> struct DistVec<double> {
 };
 
 // 256 threads = 16x16; thread (ty, tx) owns rows ty*4..+3 and cols tx*4..+3.
+// float64: 64 registers, 4 CTAs per SM (the integer-pipe arithmetic is
+// latency-bound at 3 CTAs; 5 would spill).
 template <typename Real>
-__global__ void __launch_bounds__(256) hdb_distance_kernel(const DistanceArgs args) {
+__global__ void __launch_bounds__(256, sizeof(Real) == 8 ? 4 : 1) hdb_distance_kernel(const DistanceArgs args) {
     using T = RealTraits<Real>;
     constexpr int KC = DistVec<Real>::KC;
     __shared__ __align__(16) Real s_i[KC][kDistTile];
