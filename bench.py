@@ -222,7 +222,8 @@ def sklearn_baseline(packed, offsets, params, count):
 
 def phase_report(phase_ms, phase_launches, describe, D, itemsize, peak, core_distances):
     """Distance and core phases as achieved GB/s of algorithmic bytes (against the HBM peak), the
-    forward as device ms.  Algorithmic bytes (sums over the windows of each kind):
+    distance phase also as pair-coordinates per second (its arithmetic rate), the forward as device
+    ms.  Algorithmic bytes (sums over the windows of each kind):
       distance: read X (n*D*s) + write the n x n block (n^2*s), matrix-variant windows;
       core:     matrix windows read their block (n^2*s) + write core and neighbour (n*(s+4));
                 recompute windows read X (n*D*s) + the same writes (these are SIMT-bound)."""
@@ -235,8 +236,12 @@ def phase_report(phase_ms, phase_launches, describe, D, itemsize, peak, core_dis
     dist_bytes = (n2_m + points_m * D) * itemsize
     if phase_launches["distance"]:
         gbs = dist_bytes / (phase_ms["distance"] / 1e3) / 1e9
+        pair_coords = (n2_m - points_m) // 2 * D  # distinct pairs i < j times coordinates
         out["distance"] = {"ms": phase_ms["distance"], "launches": phase_launches["distance"], "bytes": dist_bytes,
-                           "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+                           "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak,
+                           "pair_coordinates": pair_coords,
+                           "pair_coordinates_per_s": pair_coords / (phase_ms["distance"] / 1e3),
+                           "note": "arithmetic-bound: FP64 and ALU pipes (float64), FMA-pipe issue (float32)"}
     if core_distances and phase_launches["core"]:
         core_bytes = n2_m * itemsize + (points_m + points_r) * (itemsize + 4) + points_r * D * itemsize
         gbs = core_bytes / (phase_ms["core"] / 1e3) / 1e9
