@@ -422,61 +422,75 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_distinct) 
 // Single linkage (reference: _kernels.py:518-556).  Node n+i merges the
 // components of the i-th sorted edge (source side first).  Inputs: s2 sorted
 // sources, s3 sorted targets.  Outputs: s4 left, s5 right, s6 size of node n+i
-// at index i.  The words live in r1/r2; s7/s8 hold a batch's roots.
+// at index i.  The union-find words live in r1/r2.
 //
 // Edges go in batches of 32: first every lane walks its edge's two endpoints
-// to their roots in the state before the batch (in parallel), then lane 0
-// commits the batch's unions in order, reading each root's word (which it
-// needs anyway for the node id and size) and following parents only from a
-// root that an earlier union of the same batch made a child.  Only roots'
-// words ever change, so the committed roots, sizes, orientations and node ids
-// are those of the serial union-find.
+// to their roots in the state before the batch (in parallel), then the
+// batch's unions are replayed in order in registers (one shuffle broadcast of
+// the edge's two roots per step; lanes holding either root take the merged
+// one), and finally every lane writes its edge's row and its part of the
+// forest update.  The roots, sizes, orientations and node ids are those of
+// the serial union-find.
 // ---------------------------------------------------------------------------
 template <typename Real>
 __device__ void linkage_warp(const Arena<Real>& a, int n) {
     const int lane = threadIdx.x & 31;
     const int m = n - 1;
-    uint2* U = reinterpret_cast<uint2*>(a.r1);  // {parent | node << 16, size}
-    int16_t* root_x = a.s7;
-    int16_t* root_y = a.s8;
+    uint2* U = reinterpret_cast<uint2*>(a.r1);  // {parent | node << 16, size}; node and size valid at roots
     for (int x = lane; x < n; x += 32) U[x] = make_uint2((uint32_t)x | ((uint32_t)x << 16), 1u);
     __syncwarp();
     for (int base = 0; base < m; base += 32) {
-        const int i = base + lane;
-        if (i < m) {
-            int x = a.s2[i], y = a.s3[i];
-            uint32_t px = U[x].x & 0xffffu, py = U[y].x & 0xffffu;
-            while ((int)px != x || (int)py != y) {
-                x = (int)px;
-                y = (int)py;
-                px = U[x].x & 0xffffu;
-                py = U[y].x & 0xffffu;
+        const int e = base + lane;
+        const int count = min(32, m - base);
+        // 1. Each lane finds the roots of its edge's endpoints in the forest
+        //    as it stood before this batch, with their {root | node, size}.
+        uint2 wx = make_uint2(0u, 0u), wy = make_uint2(0u, 0u);
+        if (e < m) {
+            int x = a.s2[e], y = a.s3[e];
+            wx = U[x];
+            wy = U[y];
+            while ((int)(wx.x & 0xffffu) != x || (int)(wy.x & 0xffffu) != y) {
+                x = (int)(wx.x & 0xffffu);
+                y = (int)(wy.x & 0xffffu);
+                wx = U[x];
+                wy = U[y];
             }
-            root_x[lane] = (int16_t)x;
-            root_y[lane] = (int16_t)y;
         }
-        __syncwarp();
-        if (lane == 0) {
-            const int count = min(32, m - base);
-            for (int l = 0; l < count; ++l) {
-                int x = root_x[l], y = root_y[l];
-                uint2 wx = U[x], wy = U[y];
-                while ((int)(wx.x & 0xffffu) != x) { x = (int)(wx.x & 0xffffu); wx = U[x]; }
-                while ((int)(wy.x & 0xffffu) != y) { y = (int)(wy.x & 0xffffu); wy = U[y]; }
-                const int e = base + l;
-                const uint32_t sx = wx.y, sy = wy.y, s = sx + sy;
-                a.s4[e] = (int16_t)(wx.x >> 16);
-                a.s5[e] = (int16_t)(wy.x >> 16);
-                a.s6[e] = (int16_t)s;
-                const uint32_t node = (uint32_t)(n + e) << 16;
-                if (sx < sy) {
-                    U[x].x = (wx.x & 0xffff0000u) | (uint32_t)y;
-                    U[y] = make_uint2((uint32_t)y | node, s);
-                } else {
-                    U[y].x = (wy.x & 0xffff0000u) | (uint32_t)x;
-                    U[x] = make_uint2((uint32_t)x | node, s);
-                }
+        uint32_t kx = wx.x, sx = wx.y, ky = wy.x, sy = wy.y;
+        // 2. The batch's merges in edge order, resolved in registers: step l
+        //    broadcasts edge l's current roots, and every lane whose root is
+        //    one of them takes the merged root, node and size.  A tree edge
+        //    never joins a component to itself, so the two roots differ.
+        uint32_t left = 0, right = 0, size = 0, winner = 0, loser = 0;
+        bool superseded = false;  // this lane's root was merged again later in the batch
+        for (int l = 0; l < count; ++l) {
+            const uint32_t KX = __shfl_sync(0xffffffffu, kx, l), KY = __shfl_sync(0xffffffffu, ky, l);
+            const uint32_t SX = __shfl_sync(0xffffffffu, sx, l), SY = __shfl_sync(0xffffffffu, sy, l);
+            const uint32_t X = KX & 0xffffu, Y = KY & 0xffffu, S = SX + SY;
+            const uint32_t W = SX < SY ? Y : X;  // union by size, ties keep x's root
+            const uint32_t merged = W | ((uint32_t)(n + base + l) << 16);
+            if (lane == l) {
+                left = KX >> 16;
+                right = KY >> 16;
+                size = S;
+                winner = W;
+                loser = SX < SY ? X : Y;
             }
+            if (lane < l && (winner == X || winner == Y)) superseded = true;
+            const uint32_t rx = kx & 0xffffu, ry = ky & 0xffffu;
+            if (rx == X || rx == Y) { kx = merged; sx = S; }
+            if (ry == X || ry == Y) { ky = merged; sy = S; }
+        }
+        // 3. Outputs and the forest update, one lane per edge.  Every loser
+        //    is merged once, and a winner's word is written only by the last
+        //    edge of the batch that merged it, so no two lanes store to the
+        //    same word.
+        if (e < m) {
+            a.s4[e] = (int16_t)left;
+            a.s5[e] = (int16_t)right;
+            a.s6[e] = (int16_t)size;
+            U[loser].x = winner;
+            if (!superseded) U[winner] = make_uint2(winner | ((uint32_t)(n + e) << 16), size);
         }
         __syncwarp();
     }
