@@ -307,13 +307,8 @@ __device__ bool radix_sort_distinct_warp(const Arena<Real>& a, int m) {
 #pragma unroll
         for (int b = 0; b < 8; ++b) hist[8 * lane + b] = 0;
         __syncwarp();
-        for (int base = 0; base < m; base += 32) {
-            const int i = base + lane;
-            const int d = i < m ? radix_digit(kin[i], shift) : 256;
-            const unsigned same = same_digit_lanes(d);
-            if (d < 256 && (same & lt) == 0) hist[d] += __popc(same);
-            __syncwarp();
-        }
+        for (int i = lane; i < m; i += 32) atomicAdd(&hist[radix_digit(kin[i], shift)], 1);
+        __syncwarp();
         // Exclusive scan; each lane owns 8 consecutive digits.
         int local[8], sum = 0, full = 0;
 #pragma unroll
