@@ -12,7 +12,10 @@
 // Hand-off uses named barriers only (bar.arrive / bar.sync with fixed thread
 // counts): FULL[b] (Prim arrives, tree waits) and EMPTY[b] (tree arrives, Prim
 // waits before reusing arena b).  With one arena (large windows) the two
-// roles simply alternate.
+// roles simply alternate.  In matrix variants of at most 4 slots per thread
+// the next ticket is taken before each hand-off; when the CTA has no window
+// left, the Prim warps join the tree warp for that last window's sort (HELP,
+// the whole CTA) and exit, and the tree warp finishes the window alone.
 //
 // Prim details:
 //  * slot s lives in thread s / SV (vertex id vid; the matrix variant lays
@@ -44,6 +47,13 @@ constexpr int kBarStart = 1;  // Prim threads: window start / staging / post-Pri
 constexpr int kBarIter = 2;   // active Prim warps: per-iteration barrier
 constexpr int kBarFull = 3;   // 3, 4: Prim -> tree hand-off of arena 0 / 1
 constexpr int kBarEmpty = 5;  // 5, 6: tree -> Prim release of arena 0 / 1
+constexpr int kBarHelp = 7;   // whole CTA: the last window's sort with the Prim warps helping
+// A CTA's last window sorts with every warp when it has at least this many
+// edges, in matrix variants of at most 4 slots per thread: with 8 slots the
+// float32 matrix Prim measured 3.4x slower per iteration in a build with this
+// path, and the register variants keep their Prim code as measured.
+constexpr int kHelpMinEdges = 256;
+constexpr int kHelpMaxSlots = 4;
 
 __device__ __forceinline__ void bar_sync(int id, int count) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
@@ -350,7 +360,8 @@ __device__ __forceinline__ int prim_window(const ForwardArgs& args, const Arena<
 // NumPy-order sort, linkage, condensation, selection and labels
 // (reference _kernels.py:358-760), on the arena at `base`.
 template <typename Real>
-__device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char* base_ptr, int w, int n) {
+__device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char* base_ptr, int w, int n,
+                                         int* help_ctr = nullptr) {
     const int lane = threadIdx.x & 31;
     const Real epsilon = (Real)args.eps;  // the reference casts options to Real (_cuda.py:105)
     const int m = n - 1;
@@ -365,7 +376,10 @@ __device__ __noinline__ void tree_window(const ForwardArgs& args, unsigned char*
             static_cast<Real*>(args.edge_w)[ebase + i] = a.r0[i];
         }
     }
-    sort_edges_warp<Real>(a, m, args.unit_core != 0);
+    if (help_ctr)  // the Prim warps have no window left and join the sort (whole CTA)
+        sort_edges_cta<Real>(a, m, (int)blockDim.x, kBarHelp, help_ctr);
+    else
+        sort_edges_warp<Real>(a, m, args.unit_core != 0);
     if (args.stage_ns && lane == 0) args.stage_ns[8 * w + 4] = global_ns();
     if (args.order)
         for (int i = lane; i < m; i += 32) args.order[ebase + i] = a.s2[i];
@@ -418,6 +432,7 @@ struct WindowMeta {
     int w;      // window index, -1 = queue exhausted
     int n;
     int skip;   // labels already written (invalid input / overflow)
+    int help;   // the CTA's last window: the Prim warps join its sort, then both sides exit
 };
 
 // Dynamic shared memory: n_arenas arenas of arena_stride bytes, then the
@@ -436,6 +451,7 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
     static_assert(PT % 32 == 0 && PT + 32 <= 1024, "Prim threads plus the tree warp must fit one CTA");
     static_assert(SV <= 16, "in-tree bits are kept in one 16-bit mask");
     constexpr Key SENTINEL = (Key)~(Key)0;
+    constexpr bool kJoinSort = DP == 0 && SV <= kHelpMaxSlots;
 
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Key s_key[2][PW];
@@ -458,6 +474,12 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
             bar_sync(kBarFull + b, PT + 32);
             const WindowMeta meta = s_meta[b];
             if (meta.w < 0) return;
+            if constexpr (kJoinSort) {
+                if (meta.help) {  // no release: the Prim warps consumed every earlier one and exit too
+                    tree_window<Real>(args, smem + (size_t)b * args.arena_stride, meta.w, meta.n, s_scan);
+                    return;
+                }
+            }
             if (!meta.skip) tree_window<Real>(args, smem + (size_t)b * args.arena_stride, meta.w, meta.n);
             __syncwarp();
             __threadfence_block();
@@ -472,10 +494,17 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
     Real* s_x = reinterpret_cast<Real*>(smem + args.x_off);
     Real* s_core = reinterpret_cast<Real*>(smem + args.core_off);
 
+    if constexpr (kJoinSort) {
+        if (tid == 0) s_item = atomicAdd(args.ticket, 1);
+    }
     for (int k = 0; k < (1 << 30); ++k) {
         const int b = nb == 2 ? (k & 1) : 0;
         const int par = k & 1;
-        if (tid == 0) { s_item = atomicAdd(args.ticket, 1); s_flags[par] = 0; }
+        if constexpr (kJoinSort) {
+            if (tid == 0) s_flags[par] = 0;  // the ticket was taken before the last hand-off
+        } else {
+            if (tid == 0) { s_item = atomicAdd(args.ticket, 1); s_flags[par] = 0; }
+        }
         bar_sync(kBarStart, PT);
         const int item = s_item;
         if (item >= args.queue_len) {
@@ -542,6 +571,11 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
                 overflow = prim_window<Real, PT, SV, DP, false>(args, arena, s_x, s_core, Xw, Dw, n, xs, s_key, s_idx, s_scan);
         }
         if (overflow) atomicOr(&s_flags[par], overflow << 1);
+        if constexpr (kJoinSort) {
+            // The next window's ticket, taken before the hand-off so that the
+            // CTA's last window is known as such.
+            if (tid == 0) s_item = atomicAdd(args.ticket, 1);
+        }
         bar_sync(kBarStart, PT);
         const int flags = s_flags[par];
         if (args.stage_ns && tid == 0) args.stage_ns[8 * w + 2] = global_ns();
@@ -552,9 +586,21 @@ __global__ void __launch_bounds__(PT + 32, MINB) hdb_forward_kernel(const __grid
             for (int j = tid; j < n; j += PT) args.labels[base + j] = -1;
             skip = 1;
         }
-        if (tid == 0) { s_meta[b].w = w; s_meta[b].n = n; s_meta[b].skip = skip; }
+        int help = 0;
+        if constexpr (kJoinSort)
+            help = s_item >= args.queue_len && !skip && !args.unit_core && n - 1 >= kHelpMinEdges;
+        if (tid == 0) { s_meta[b].w = w; s_meta[b].n = n; s_meta[b].skip = skip; s_meta[b].help = help; }
         __threadfence_block();
         bar_arrive(kBarFull + b, PT + 32);
+        if constexpr (kJoinSort) {
+            if (help) {
+                // Take the tree warp's release of the previous window (nothing
+                // may stay pending at exit), then sort this one with it.
+                if (nb == 2 && k >= 1) bar_sync(kBarEmpty + (b ^ 1), PT + 32);
+                sort_edges_cta<Real>(arena, n - 1, PT + 32, kBarHelp, s_scan);
+                return;
+            }
+        }
     }
 }
 

@@ -413,6 +413,72 @@ __device__ void sort_edges_warp(const Arena<Real>& a, int m, bool try_distinct) 
     __syncwarp();
 }
 
+// The same sort by every warp of the CTA (`nthreads` threads, all of which
+// must call; the named barrier `bar` spans them): the partition tasks go in
+// rounds, each warp taking every nw-th task of the round, and the lane
+// segments are shared by all threads.  Segments are disjoint and each one's
+// partition depends only on its own bounds and depth code, so the result
+// equals the one-warp form's.  ctr: four ints of shared memory.
+template <typename Real>
+__device__ __forceinline__ void sort_edges_cta(const Arena<Real>& a, int m, int nthreads, int bar, int* ctr) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = nthreads >> 5;
+    SortPair<Real>* p = reinterpret_cast<SortPair<Real>*>(a.r1);
+    for (int i = tid; i < m; i += nthreads) { p[i].w = a.r0[i]; p[i].idx = i; }
+    int16_t *task_lo = a.s5, *task_hi = a.s6, *task_depth = a.s7;  // two halves: this round, next round
+    int16_t *leaf_lo = a.s8, *leaf_hi = a.s9, *leaf_code = a.s2;
+    const int half = Arena<Real>::round_cap(m + 1) / 2;
+    const int lane_max = 33;
+    if (tid == 0) {
+        int depth = 0;
+        for (int c = m; c > 1; c >>= 1) depth += 2;  // 2*floor(log2(m)), _kernels.py:429-431
+        task_lo[0] = 0;
+        task_hi[0] = (int16_t)(m - 1);
+        task_depth[0] = (int16_t)(depth * 2 + 1);
+        ctr[0] = 0; ctr[1] = 0; ctr[2] = 0; ctr[3] = 0;  // pushes of rounds r % 3; leaves
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+    int count = m > 1 ? 1 : 0;
+    for (int round = 0; count > 0; ++round) {
+        const int cur = (round & 1) * half, nxt = half - cur;
+        int* pushes = ctr + round % 3;
+        if (tid == 0) ctr[(round + 1) % 3] = 0;  // last read two barriers ago
+        for (int t = warp; t < count; t += nw) {
+            const int lo = task_lo[cur + t], hi = task_hi[cur + t], code = task_depth[cur + t];
+            const int depth = code >> 1;  // arithmetic shift keeps negative depths
+            const bool checked = code & 1;
+            if ((checked && depth < 0) || hi - lo + 1 < lane_max) {
+                if (lane == 0) {
+                    const int k = atomicAdd(ctr + 3, 1);
+                    leaf_lo[k] = (int16_t)lo; leaf_hi[k] = (int16_t)hi; leaf_code[k] = (int16_t)code;
+                }
+            } else {
+                const int i = partition_warp(p, lo, hi, a.s3, a.s4);
+                const int d = depth - 1;
+                int big_lo, big_hi, small_lo, small_hi;
+                if (i - lo < hi - i) { big_lo = i + 1; big_hi = hi; small_lo = lo; small_hi = i - 1; }
+                else { big_lo = lo; big_hi = i - 1; small_lo = i + 1; small_hi = hi; }
+                if (lane == 0) {
+                    const int k = nxt + atomicAdd(pushes, 2);
+                    task_lo[k] = (int16_t)big_lo; task_hi[k] = (int16_t)big_hi; task_depth[k] = (int16_t)(d * 2 + 1);
+                    task_lo[k + 1] = (int16_t)small_lo; task_hi[k + 1] = (int16_t)small_hi;
+                    task_depth[k + 1] = (int16_t)(d * 2);
+                }
+            }
+            __syncwarp();
+        }
+        asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+        count = *pushes;
+    }
+    const int leaves = ctr[3];
+    for (int t = tid; t < leaves; t += nthreads) introsort_lane(p, leaf_lo[t], leaf_hi[t], leaf_code[t]);
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+    for (int i = tid; i < m; i += nthreads) {
+        a.s2[i] = (int16_t)p[i].idx;
+        a.r0[i] = p[i].w;
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Single linkage (reference: _kernels.py:518-556).  Node n+i merges the
 // components of the i-th sorted edge (source side first).  Inputs: s2 sorted
