@@ -75,8 +75,12 @@ class ClockSampler:
         try:
             self.file = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.file, stderr=subprocess.DEVNULL)
+            # Start the timed region only once the sampler is writing (at most 3 s).
+            deadline = time.perf_counter() + 3.0
+            while time.perf_counter() < deadline and self.proc.poll() is None and self.path.stat().st_size == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
